@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""SCAN on R-MAT scale 22 (edge factor 16, a/b/c/d = .57/.19/.19/.05, seed 1), eps=0.5, mu=5.
+
+Metric: similarity edges/s -- undirected edges classified (common neighbours counted, eps
+tested) and clustered per second.  One step = one full SCAN pass (similarity, predicate,
+cores, union-find, attach, hub/outlier) over the graph.
+
+  value     device time, graph resident in HBM (CUDA events on the library's stream)
+  e2e       the reference-facing drop-in GPUScan() (scan_gpuscan_compat) from pinned host
+            CSR buffers to host labels: H2D, orientation, SCAN, D2H and device allocation
+  roofline  the common-neighbour stage, HBM bound
+  cpu_baseline  the oracle (a plain OpenMP merge-intersection SCAN) on a bounded edge sample
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has
+no exchange step); value = all ranks' edges / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "rmat-s22-ef16-scan"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--eps", default="0.5")
+    ap.add_argument("--mu", type=int, default=5)
+    ap.add_argument("--predicate", default="ref-f64", choices=["ref-f64", "exact"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduce across replicas (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        dev = "cuda" if self.dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.file.name)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(deg: np.ndarray, E: int) -> dict:
+    """Bytes per launch of the common-neighbour stage.
+
+    merge model (the per-edge figure of the survey): each edge streams both lists,
+      B = sum_e [4 (du + dv) + 16] + 4 E = 4 sum_v d_v^2 + 20 E.
+    probe model (the lists this kernel must read): each edge streams the lower endpoint's
+      list once (min(du, dv)), each pivot list is staged once, plus per-edge offsets,
+      endpoint and count: B = 4 sum_e min(du, dv) + 4 sum_v d_v + 16 E.
+    """
+    d = deg.astype(np.float64)
+    merge = 4.0 * float((d * d).sum()) + 20.0 * E
+    return {"merge": merge, "d2": float((d * d).sum())}
+
+
+def probe_bytes(off: np.ndarray, adj: np.ndarray) -> float:
+    deg = np.diff(off).astype(np.int64)
+    n = deg.size
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    du = deg[src]
+    dv = deg[adj.astype(np.int64)]
+    # each undirected edge appears twice; count it from its higher endpoint only
+    lower = (dv < du) | ((dv == du) & (adj.astype(np.int64) < src))
+    s_min = float(dv[lower].sum())
+    E = int(lower.sum())
+    return 4.0 * s_min + 4.0 * float(deg.sum()) + 16.0 * E
+
+
+def cpu_baseline(g, eps: str, mu: int, mode: int, seconds: float) -> dict:
+    """The oracle's merge intersection + predicate on a uniform edge sample, all host cores."""
+    from oracle import oracle
+
+    off, adj = g.offsets(), g.adjacency()
+    eu, ev = oracle.orient(off, adj)
+    E = eu.size
+    rng = np.random.default_rng(1234)
+    lib = oracle.lib()
+    import ctypes as C
+
+    def run(k):
+        idx = np.sort(rng.choice(E, size=k, replace=False))
+        su, sv = np.ascontiguousarray(eu[idx]), np.ascontiguousarray(ev[idx])
+        cn = np.zeros(k, np.uint32)
+        t = time.perf_counter()
+        lib.oracle_common_neighbors(off.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                    adj.ctypes.data_as(C.POINTER(C.c_uint32)), k,
+                                    su.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                    sv.ctypes.data_as(C.POINTER(C.c_uint32)), cn.ctypes.data_as(C.POINTER(C.c_uint32)))
+        return time.perf_counter() - t
+
+    k = min(E, 20000)
+    dt = run(k)
+    k = int(min(E, max(k, k * seconds / max(dt, 1e-6))))
+    dt = run(k)
+    return {"value": k / dt, "unit": "similarity edges/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{k} of {E} edges drawn uniformly (seed 1234), oracle merge intersection, "
+                      f"OpenMP on {os.cpu_count()} threads, {dt:.1f} s"}
+
+
+def reference_arm(args) -> None:
+    """The reference path on the host cores.  GPUSCAN++ has no CPU implementation, so the
+    oracle port (its restatement) stands in: each step counts common neighbours on a fixed
+    uniform edge sample; value = sampled edges / s."""
+    import efficientstructuralgraphclusteringongpus_gb300 as sg
+    from oracle import oracle
+
+    g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
+    off, adj = g.offsets(), g.adjacency()
+    eu, ev = oracle.orient(off, adj)
+    E = eu.size
+    rng = np.random.default_rng(1234)
+    k = min(E, 200000)
+    idx = np.sort(rng.choice(E, size=k, replace=False))
+    su, sv = np.ascontiguousarray(eu[idx]), np.ascontiguousarray(ev[idx])
+    import ctypes as C
+
+    lib = oracle.lib()
+    cn = np.zeros(k, np.uint32)
+
+    def step():
+        lib.oracle_common_neighbors(off.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                    adj.ctypes.data_as(C.POINTER(C.c_uint32)), k,
+                                    su.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                    sv.ctypes.data_as(C.POINTER(C.c_uint32)), cn.ctypes.data_as(C.POINTER(C.c_uint32)))
+
+    for _ in range(args.warmup):
+        step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t
+    v = k * args.steps / dt
+    sample = f"{k} of {E} edges drawn uniformly (seed 1234) per step, oracle merge intersection, OpenMP"
+    print(json.dumps({
+        "impl": "reference", "metric": "similarity edges/s", "value": v, "unit": "similarity edges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor, "eps": args.eps,
+                   "mu": args.mu, "sample_edges": k},
+        "cpu_baseline": {"value": v, "unit": "similarity edges/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "similarity edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "GPUSCAN++ has no CPU path; the oracle's restatement is timed on the host cores",
+    }))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+    import torch
+
+    import efficientstructuralgraphclusteringongpus_gb300 as sg
+
+    torch.cuda.set_device(local)
+    dist = Dist(world, "nccl")
+    mode = sg.PRED_REF_F64 if args.predicate == "ref-f64" else sg.PRED_EXACT
+
+    g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
+    n, E = g.n, g.num_edges
+    off, adj = g.offsets(), g.adjacency()
+    g.upload(local)
+
+    # -- device-resident SCAN steps --------------------------------------------------------
+    for _ in range(args.warmup):
+        g.run(args.eps, args.mu, mode, device=local)
+    clocks = ClockSampler(local)
+    if rank == 0:
+        clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stats = []
+    for _ in range(args.steps):
+        stats.append(g.run(args.eps, args.mu, mode, device=local).stats)
+    torch.cuda.synchronize()
+    dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop() if rank == 0 else None
+    dev_ms = sum(s["ms_similarity"] + s["ms_cluster"] for s in stats)
+    dev_ms = dist.max(dev_ms)
+    sim_ms = [s["ms_similarity"] for s in stats]
+    launches = sum(s["kernel_launches"] for s in stats)
+    value = world * E * args.steps / (dev_ms / 1e3)
+    last = stats[-1]
+
+    # -- end to end through the drop-in GPUScan with pinned host buffers ----------------------
+    off32 = torch.from_numpy(off.astype(np.uint32).view(np.int32)).pin_memory()
+    adj32 = torch.from_numpy(adj.view(np.int32)).pin_memory()
+    h_off = off32.numpy().view(np.uint32)
+    h_adj = adj32.numpy()
+    sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)   # warm
+    dist.barrier()
+    t = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        out = sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)
+    e2e_s = dist.max(time.perf_counter() - t)
+    e2e_value = world * E * args.e2e_steps / e2e_s
+    check = g.run(args.eps, args.mu, sg.PRED_REF_F64, device=local).label
+    e2e_matches = bool(np.array_equal(out, check))
+
+    # -- roofline of the common-neighbour stage -------------------------------------------
+    deg = np.diff(off).astype(np.int64)
+    ab = algorithmic_bytes(deg, E)
+    pb = probe_bytes(off, adj)
+    peaks_file = ROOT / "MEASURED_PEAKS.json"
+    if peaks_file.exists():
+        peak = float(json.loads(peaks_file.read_text())["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    sim_s = float(np.mean(sim_ms)) / 1e3
+    roof = {"bound": "hbm", "achieved": ab["merge"] / sim_s / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": ab["merge"] / sim_s / 1e9 / peak, "traffic": None, "peak_source": peak_src,
+            "bytes_model": "merge: 4*sum_v d_v^2 + 20E (both lists per edge)",
+            "probe_model": {"achieved": pb / sim_s / 1e9, "frac": pb / sim_s / 1e9 / peak,
+                            "bytes": pb, "definition": "4*sum_e min(du,dv) + 4*sum_v d_v + 16E"},
+            "kernel_ms": sim_s * 1e3}
+
+    result = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(g, args.eps, args.mu, mode, args.cpu_seconds)
+        result = {
+            "metric": "similarity edges/s", "value": value, "unit": "similarity edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "undirected_edges": E, "max_degree": g.max_degree,
+                       "eps": args.eps, "mu": args.mu, "predicate": args.predicate,
+                       "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (adjacency 4*m bytes)"},
+            "e2e": {"value": e2e_value, "unit": "similarity edges/s", "h2d_bytes_per_step": int(4 * (n + 1) + 4 * g.m),
+                    "d2h_bytes_per_step": int(4 * n), "api": "GPUScan drop-in (scan_gpuscan_compat)",
+                    "ms_per_step": e2e_s / args.e2e_steps * 1e3, "labels_match_resident_run": e2e_matches},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+            "stages_ms": {"similarity": float(np.mean(sim_ms)),
+                          "cluster": float(np.mean([s["ms_cluster"] for s in stats])),
+                          "d2h": float(np.mean([s["ms_d2h"] for s in stats])),
+                          "wall_per_step": wall / args.steps * 1e3},
+            "scan": {"cores": last["num_cores"], "clusters": last["num_clusters"], "borders": last["num_borders"],
+                     "hubs": last["num_hubs"], "outliers": last["num_outliers"],
+                     "similar_edges": last["num_similar_edges"],
+                     "predicate_disagreements": last["pred_disagreements"]},
+        }
+        print(json.dumps(result))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,241 @@
+// From common-neighbour counts to clusters: predicate, cores, union-find, attachment,
+// hub/outlier classification.  All passes are edge-parallel over the E undirected edges
+// (lo_adj/lo_src) or vertex-parallel; per-vertex arrays (n x 4 B) stay L2-resident.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace scan {
+
+// ---- the epsilon predicate -------------------------------------------------------------
+// u is the lower endpoint in (degree, id) order, v the higher; t = |N(u) ∩ N(v)|.
+//
+// ref-f64 reproduces, with the same operand order, the reference's three double tests:
+//   'N' prune  deg_u < deg_v * eps * eps                      GPUSCAN++/GPUScan.cu:145
+//   'Y' prune  eps * eps * deg_u * deg_v <= 4.0               GPUSCAN++/GPUScan.cu:156
+//   intersect  (T+2)*(T+2) < eps * eps * (du+1) * (dv+1)      GPUSCAN++/GPUScan.cu:220-221
+// with deg_x = d_x + 1 and (T+2)*(T+2) an int product (wraps past 46340).  The 'Y' prune
+// agrees with the intersect test whenever it fires ((T+2)^2 >= 4), so it is implied.
+// Only IEEE multiplies and compares are used: no contraction, identical bits on any host.
+__host__ __device__ __forceinline__ bool ref_f64_similar(uint32_t t, uint32_t du, uint32_t dv, double eps) {
+    const double du1 = (double)(du + 1u), dv1 = (double)(dv + 1u);
+    if (du1 < dv1 * eps * eps) return false;
+    const int32_t t2 = (int32_t)((t + 2u) * (t + 2u));
+    return !((double)t2 < eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u));
+}
+
+// exact: (t+2)^2 * q^2 >= p^2 * (du+1) * (dv+1) with eps = p/q, p <= q <= 2^30.
+// (t+2)*q < 2^63 and p^2 < 2^60, so both sides fit 128 bits.
+__host__ __device__ __forceinline__ bool exact_similar(uint32_t t, uint32_t du, uint32_t dv, uint64_t p, uint64_t q) {
+    if (p > q) return false;  // sigma <= 1 < eps
+    const uint64_t a = (uint64_t)(t + 2ull) * q;
+    const unsigned __int128 lhs = (unsigned __int128)a * a;
+    const unsigned __int128 rhs = (unsigned __int128)(p * p) * ((uint64_t)(du + 1ull) * (uint64_t)(dv + 1ull));
+    return lhs >= rhs;
+}
+
+struct PredParams {
+    double eps;          // ref-f64 value (strtod of the decimal text, like atof in main.cpp:26)
+    uint64_t p, q;       // exact value p/q
+    int mode;            // 0 exact, 1 ref-f64
+};
+
+// sim[e] and the similar-degree count sd[] of both endpoints (core rule: a vertex is a
+// core when at least mu of its neighbours are similar, GPUSCAN++/GPUScan.cu:147-165).
+// Edges of one pivot are contiguous, so the pivot side is summed per warp segment.
+__global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                            const uint32_t* __restrict__ off, const uint32_t* __restrict__ cn, PredParams pp,
+                            uint8_t* __restrict__ sim, int32_t* __restrict__ sd, RunCounters* __restrict__ ctr) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long nsim = 0, ndis = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t e0 = (uint64_t)blockIdx.x * blockDim.x; e0 < E; e0 += stride) {
+        const uint64_t e = e0 + threadIdx.x;
+        bool s = false;
+        uint32_t v = kEmpty;
+        if (e < E) {
+            const uint32_t u = lo_adj[e];
+            v = lo_src[e];
+            const uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
+            const uint32_t t = cn[e];
+            const bool r = ref_f64_similar(t, du, dv, pp.eps);
+            const bool x = exact_similar(t, du, dv, pp.p, pp.q);
+            s = pp.mode ? r : x;
+            ndis += (r != x);
+            nsim += s;
+            sim[e] = s;
+            if (s) atomicAdd(&sd[u], 1);
+        }
+        // pivot side: one atomic per run of equal pivots within the warp
+        const uint32_t key = s ? v : kEmpty;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (s && (__ffs(peers) - 1) == (int)lane) atomicAdd(&sd[v], __popc(peers));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nsim += __shfl_xor_sync(0xFFFFFFFFu, nsim, o);
+        ndis += __shfl_xor_sync(0xFFFFFFFFu, ndis, o);
+    }
+    if (lane == 0) {
+        if (nsim) atomicAdd(&ctr->similar_edges, nsim);
+        if (ndis) atomicAdd(&ctr->disagreements, ndis);
+    }
+}
+
+// parent[v] = v for cores, -1 otherwise; border/neighbour label ranges reset.
+__global__ void k_core_init(uint32_t n, const int32_t* __restrict__ sd, int mu, int32_t* __restrict__ parent,
+                            int32_t* __restrict__ bmin, int32_t* __restrict__ bmax, int32_t* __restrict__ nmin,
+                            int32_t* __restrict__ nmax) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        parent[v] = sd[v] >= mu ? (int32_t)v : -1;
+        bmin[v] = 0x7FFFFFFF;
+        bmax[v] = -1;
+        nmin[v] = 0x7FFFFFFF;
+        nmax[v] = -1;
+    }
+}
+
+// Root of x with path halving.  parent[y] < y for every non-root y, so every write keeps
+// the forest acyclic and the walk terminates.
+__device__ __forceinline__ int32_t uf_find(volatile int32_t* parent, int32_t x) {
+    int32_t p = parent[x];
+    while (p != x) {
+        const int32_t g = parent[p];
+        if (g != p) parent[x] = g;
+        x = p;
+        p = g;
+    }
+    return x;
+}
+
+// Lock-free union by smaller root id: the root of a component is its smallest core id,
+// which is the reference's cluster id (GPUSCAN++/GPUScan.cu:500-523 hooks the larger
+// root under the smaller one).
+__device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b) {
+    volatile int32_t* vp = parent;
+    for (int it = 0; it < (1 << 20); ++it) {
+        a = uf_find(vp, a);
+        b = uf_find(vp, b);
+        if (a == b) return true;
+        if (a < b) { const int32_t t = a; a = b; b = t; }   // a > b: hang a under b
+        if (atomicCAS(&parent[a], a, b) == a) return true;
+    }
+    return false;
+}
+
+__global__ void k_union(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                        const uint8_t* __restrict__ sim, int32_t* parent, RunCounters* ctr) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        if (!sim[e]) continue;
+        const int32_t u = (int32_t)lo_adj[e], v = (int32_t)lo_src[e];
+        if (parent[u] < 0 || parent[v] < 0) continue;   // core-core only (cores never change)
+        if (!uf_union(parent, u, v)) atomicOr(&ctr->error_flags, kErrUnionFindLimit);
+    }
+}
+
+__global__ void k_flatten(uint32_t n, int32_t* parent) {
+    volatile int32_t* vp = parent;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        if (vp[v] >= 0) {
+            const int32_t r = uf_find(vp, (int32_t)v);
+            vp[v] = r;
+        }
+    }
+}
+
+// Border attachment: a non-core similar to a core joins that core's cluster.  The
+// reference keeps the last write among several clusters (GPUSCAN++/GPUScan.cu:716,722);
+// here the smallest cluster id wins, and bmin != bmax marks a multi-cluster border.
+__global__ void k_attach(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                         const uint8_t* __restrict__ sim, const int32_t* __restrict__ parent,
+                         int32_t* __restrict__ bmin, int32_t* __restrict__ bmax) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        if (!sim[e]) continue;
+        const uint32_t u = lo_adj[e], v = lo_src[e];
+        const int32_t pu = parent[u], pv = parent[v];
+        if (pu >= 0 && pv < 0) { atomicMin(&bmin[v], pu); atomicMax(&bmax[v], pu); }
+        else if (pv >= 0 && pu < 0) { atomicMin(&bmin[u], pv); atomicMax(&bmax[u], pv); }
+    }
+}
+
+// Label after attachment: cluster id for cores and borders, -2 for the rest.
+__global__ void k_label(uint32_t n, const int32_t* __restrict__ parent, const int32_t* __restrict__ bmin,
+                        int32_t* __restrict__ lab) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const int32_t p = parent[v];
+        lab[v] = p >= 0 ? p : (bmin[v] != 0x7FFFFFFF ? bmin[v] : -2);
+    }
+}
+
+// Hub test inputs: for each unlabelled vertex, the smallest and largest label among its
+// neighbours.  Two distinct labels make it a hub (GPUSCAN++/GPUScan.cu:757-780 looks for a
+// second neighbour label different from the first).
+__global__ void k_neighbour_labels(uint64_t E, const uint32_t* __restrict__ lo_adj,
+                                   const uint32_t* __restrict__ lo_src, const int32_t* __restrict__ lab,
+                                   int32_t* __restrict__ nmin, int32_t* __restrict__ nmax) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t u = lo_adj[e], v = lo_src[e];
+        const int32_t lu = lab[u], lv = lab[v];
+        if (lu < 0 && lv >= 0) { atomicMin(&nmin[u], lv); atomicMax(&nmax[u], lv); }
+        else if (lv < 0 && lu >= 0) { atomicMin(&nmin[v], lu); atomicMax(&nmax[v], lu); }
+    }
+}
+
+// Final labels, roles and counters.
+__global__ void k_finalize(uint32_t n, const int32_t* __restrict__ parent, const int32_t* __restrict__ bmin,
+                           const int32_t* __restrict__ bmax, const int32_t* __restrict__ nmin,
+                           const int32_t* __restrict__ nmax, int32_t* __restrict__ label,
+                           uint8_t* __restrict__ role, RunCounters* __restrict__ ctr) {
+    unsigned long long c_core = 0, c_clu = 0, c_hub = 0, c_out = 0, c_bor = 0, c_multi = 0;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const int32_t p = parent[v];
+        int32_t l;
+        uint8_t r;
+        if (p >= 0) {
+            l = p; r = kRoleCore; ++c_core; c_clu += (p == (int32_t)v);
+        } else if (bmin[v] != 0x7FFFFFFF) {
+            l = bmin[v]; r = kRoleBorder; ++c_bor; c_multi += (bmin[v] != bmax[v]);
+        } else if (nmin[v] < nmax[v]) {
+            l = -1; r = kRoleHub; ++c_hub;
+        } else {
+            l = -2; r = kRoleOutlier; ++c_out;
+        }
+        label[v] = l;
+        if (role) role[v] = r;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c_core += __shfl_xor_sync(0xFFFFFFFFu, c_core, o);
+        c_clu += __shfl_xor_sync(0xFFFFFFFFu, c_clu, o);
+        c_hub += __shfl_xor_sync(0xFFFFFFFFu, c_hub, o);
+        c_out += __shfl_xor_sync(0xFFFFFFFFu, c_out, o);
+        c_bor += __shfl_xor_sync(0xFFFFFFFFu, c_bor, o);
+        c_multi += __shfl_xor_sync(0xFFFFFFFFu, c_multi, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c_core) atomicAdd(&ctr->cores, c_core);
+        if (c_clu) atomicAdd(&ctr->clusters, c_clu);
+        if (c_hub) atomicAdd(&ctr->hubs, c_hub);
+        if (c_out) atomicAdd(&ctr->outliers, c_out);
+        if (c_bor) atomicAdd(&ctr->borders, c_bor);
+        if (c_multi) atomicAdd(&ctr->multi_borders, c_multi);
+    }
+}
+
+// Memberships: every (cluster, border) pair from similar core-border edges.
+__global__ void k_border_pairs(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                               const uint8_t* __restrict__ sim, const int32_t* __restrict__ parent,
+                               unsigned long long* __restrict__ count, unsigned long long* __restrict__ out,
+                               unsigned long long cap) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        if (!sim[e]) continue;
+        const uint32_t u = lo_adj[e], v = lo_src[e];
+        const int32_t pu = parent[u], pv = parent[v];
+        unsigned long long key;
+        if (pu >= 0 && pv < 0) key = ((unsigned long long)(uint32_t)pu << 32) | v;
+        else if (pv >= 0 && pu < 0) key = ((unsigned long long)(uint32_t)pv << 32) | u;
+        else continue;
+        const unsigned long long i = atomicAdd(count, 1ull);
+        if (i < cap) out[i] = key;
+    }
+}
+
+}  // namespace scan

@@ -1,0 +1,219 @@
+// Common-neighbour counting: cn[e] = |N(u) ∩ N(v)| for every undirected edge e = {u, v}.
+//
+// The reference counts each edge with a warp whose lanes binary-search the shorter list
+// in the longer one (GPUSCAN++/GPUScan.cu:174-222), once per edge and again lazily in
+// the link and attach phases (:579-584, :701-706).  Here every edge is counted exactly
+// once, grouped by its higher endpoint v (the pivot):
+//   1. the pivot's list N(v) (or one id-range chunk of it) is inserted into an
+//      open-addressing hash table in shared memory (load factor <= 1/2);
+//   2. warps stream the lower endpoints' lists N(u) with 16-byte loads and probe each
+//      element against the table; a warp reduction gives the count.
+// Per edge this reads deg(u) <= deg(v) entries, the shorter list, once; the longer
+// list is read once per task, not once per edge.
+//
+// Work is cut into tasks (pivot, chunk of N(v), slice of the pivot's edges):
+//   * small pivots (deg <= kSmallDeg): one warp per pivot, a 256-slot table per warp;
+//   * larger pivots: one CTA per task; pivots above kChunkMax entries are split into
+//     id-range chunks, each probed by the matching sub-range of N(u) (binary search),
+//     and the partial counts are added atomically.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace scan {
+
+constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single warp
+constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
+constexpr uint32_t kChunkMax = 12288;      // max pivot entries staged by one CTA
+constexpr int kNumBigClasses = 3;          // table capacities for chunk sizes below
+__host__ __device__ constexpr uint32_t big_class_entries(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : kChunkMax; }
+__host__ __device__ constexpr uint32_t big_class_slots(int c) { return 2u * big_class_entries(c); }
+
+struct CnTask {
+    uint32_t v;      // pivot
+    uint32_t cb;     // chunk of N(v): adjacency positions [cb, ce)
+    uint32_t ce;
+    uint32_t e0;     // edge slice [e0, e1) of the pivot
+    uint32_t e1;
+    uint32_t chunked;  // 1 when N(v) is split (partial counts are added atomically)
+    uint32_t pad0, pad1;
+};
+
+// Insert w into a table of `cap` slots (never full: load <= 1/2).
+__device__ __forceinline__ void table_insert(uint32_t* tab, uint32_t cap, uint32_t w) {
+    uint32_t s = hash_slot(w, cap);
+    for (uint32_t it = 0; it < cap; ++it) {
+        const uint32_t old = atomicCAS(&tab[s], kEmpty, w);
+        if (old == kEmpty || old == w) return;
+        s = (s + 1 == cap) ? 0 : s + 1;
+    }
+}
+
+__device__ __forceinline__ uint32_t table_has(const uint32_t* tab, uint32_t cap, uint32_t w) {
+    uint32_t s = hash_slot(w, cap);
+    for (uint32_t it = 0; it < cap; ++it) {
+        const uint32_t k = tab[s];
+        if (k == w) return 1u;
+        if (k == kEmpty) return 0u;
+        s = (s + 1 == cap) ? 0 : s + 1;
+    }
+    return 0u;
+}
+
+// Count elements of adj[b, e) present in the table, 16-byte loads, one warp.
+// adj is padded by >= 4 entries past m and its base is 16-byte aligned.
+__device__ __forceinline__ uint32_t warp_probe_range(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
+                                                     const uint32_t* tab, uint32_t cap, uint32_t lane) {
+    uint32_t c = 0;
+    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128) {
+        const uint4 x = __ldg(reinterpret_cast<const uint4*>(adj + p));
+        if (p >= b) c += table_has(tab, cap, x.x);
+        if (p + 1 >= b && p + 1 < e) c += table_has(tab, cap, x.y);
+        if (p + 2 >= b && p + 2 < e) c += table_has(tab, cap, x.z);
+        if (p + 3 >= b && p + 3 < e) c += table_has(tab, cap, x.w);
+    }
+    return c;
+}
+
+// First position in adj[b, e) whose value is >= key (scalar, uniform across the warp).
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
+                                                    uint32_t key) {
+    while (b < e) {
+        const uint32_t mid = b + ((e - b) >> 1);
+        if (__ldg(adj + mid) < key) b = mid + 1; else e = mid;
+    }
+    return b;
+}
+
+// Small pivots: one warp per pivot, the pivot's list in a per-warp table.
+template <int kWarpsPerBlock>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
+           const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
+           const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+    __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* tab = tabs[wib];
+    const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+    for (uint32_t t = blockIdx.x * kWarpsPerBlock + wib; t < npiv; t += nwarps) {
+        const uint32_t v = pivots[t];
+        const uint32_t b = off[v], e = off[v + 1];
+#pragma unroll
+        for (uint32_t i = lane; i < kSmallSlots; i += 32) tab[i] = kEmpty;
+        __syncwarp();
+        for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
+        __syncwarp();
+        const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
+        for (uint32_t k = k0; k < k1; ++k) {
+            const uint32_t u = lo_adj[k];
+            const uint32_t ub = off[u], ue = off[u + 1];
+            uint32_t c = 0;
+            for (uint32_t j = ub + lane; j < ue; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
+            c = __reduce_add_sync(0xFFFFFFFFu, c);
+            if (lane == 0) cn[k] = c;
+        }
+        __syncwarp();
+    }
+}
+
+// Larger pivots: one CTA per task; table of `cap` slots in dynamic shared memory.
+__global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
+                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                         const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+    extern __shared__ uint32_t tab[];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const CnTask tk = tasks[t];
+        for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) tab[i] = kEmpty;
+        __syncthreads();
+        for (uint32_t j = tk.cb + threadIdx.x; j < tk.ce; j += blockDim.x) table_insert(tab, cap, adj[j]);
+        __syncthreads();
+        const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
+        const uint32_t lo_id = (tk.cb > vb) ? adj[tk.cb] : 0u;          // chunk id range
+        const uint32_t hi_id = (tk.ce < ve) ? adj[tk.ce - 1] : kEmpty;
+        for (uint32_t k = tk.e0 + wib; k < tk.e1; k += nw) {
+            const uint32_t u = lo_adj[k];
+            uint32_t ub = off[u], ue = off[u + 1];
+            if (tk.chunked) {
+                if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
+                if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
+            }
+            uint32_t c = warp_probe_range(adj, ub, ue, tab, cap, lane);
+            c = __reduce_add_sync(0xFFFFFFFFu, c);
+            if (lane == 0) {
+                if (tk.chunked) atomicAdd(&cn[k], c); else cn[k] = c;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Task planner.  Pass 1 (tasks == nullptr) counts tasks per class; pass 2 writes them.
+// counts[0] = small pivots, counts[1 + c] = tasks of big class c.
+struct PlanParams {
+    unsigned long long target_probes;   // probe work per big task
+    uint32_t min_slice_edges;
+};
+
+__global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ lo_off,
+                       const unsigned long long* __restrict__ work, PlanParams pp,
+                       uint32_t* __restrict__ counts, uint32_t* __restrict__ small_out,
+                       CnTask* __restrict__ big0, CnTask* __restrict__ big1, CnTask* __restrict__ big2) {
+    __shared__ uint32_t blk[1 + kNumBigClasses];
+    __shared__ uint32_t base[1 + kNumBigClasses];
+    if (threadIdx.x < 1 + kNumBigClasses) blk[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    int cls = -1;
+    uint32_t ntask = 0, nch = 0, nsl = 0, L = 0, dv = 0;
+    if (v < n) {
+        L = lo_off[v + 1] - lo_off[v];
+        dv = off[v + 1] - off[v];
+        if (L > 0) {
+            if (dv <= kSmallDeg) {
+                cls = 0;
+                ntask = 1;
+            } else {
+                nch = (dv + kChunkMax - 1) / kChunkMax;
+                const uint32_t ce = (dv + nch - 1) / nch;
+                cls = 1 + (ce <= big_class_entries(0) ? 0 : ce <= big_class_entries(1) ? 1 : 2);
+                unsigned long long w = work[v] / nch;   // probes per chunk (ids spread evenly)
+                unsigned long long s = (w + pp.target_probes - 1) / pp.target_probes;
+                const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
+                nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
+                ntask = nch * nsl;
+            }
+        }
+    }
+    uint32_t mine = 0;
+    if (cls >= 0) mine = atomicAdd(&blk[cls], ntask);
+    __syncthreads();
+    if (threadIdx.x < 1 + kNumBigClasses) base[threadIdx.x] = atomicAdd(&counts[threadIdx.x], blk[threadIdx.x]);
+    __syncthreads();
+    if (cls < 0 || (small_out == nullptr)) return;
+    const uint32_t pos = base[cls] + mine;
+    if (cls == 0) {
+        small_out[pos] = v;
+        return;
+    }
+    CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : big2;
+    const uint32_t vb = off[v], e0 = lo_off[v];
+    uint32_t i = 0;
+    for (uint32_t c = 0; c < nch; ++c) {
+        const uint32_t cb = vb + (uint32_t)((uint64_t)dv * c / nch);
+        const uint32_t cend = vb + (uint32_t)((uint64_t)dv * (c + 1) / nch);
+        for (uint32_t s = 0; s < nsl; ++s, ++i) {
+            CnTask t;
+            t.v = v;
+            t.cb = cb;
+            t.ce = cend;
+            t.e0 = e0 + (uint32_t)((uint64_t)L * s / nsl);
+            t.e1 = e0 + (uint32_t)((uint64_t)L * (s + 1) / nsl);
+            t.chunked = nch > 1;
+            t.pad0 = t.pad1 = 0;
+            out[pos + i] = t;
+        }
+    }
+}
+
+}  // namespace scan

@@ -1,0 +1,145 @@
+// Orientation of the undirected edges and the exclusive scan used to lay them out.
+//
+// Every undirected edge {u, v} is stored once, under its higher endpoint v in
+// (degree, id) order -- the "pivot" whose neighbour list the similarity kernel stages in
+// shared memory.  The lower endpoint u is the same vertex the reference stores as
+// Edge_u (GPUSCAN++/Graph.cpp:66-111); only the grouping differs (the reference groups
+// edge ids by the lower endpoint, this layout by the higher one).
+//
+// HBM layout built here (all uint32):
+//   lo_off[n+1]  edges of pivot v are e in [lo_off[v], lo_off[v+1])
+//   lo_adj[E]    lower endpoint u of edge e (ascending id within a pivot)
+//   lo_src[E]    pivot v of edge e
+//   work[n]      sum of deg(u) over the lower neighbours of v (probe count of pivot v), u64
+#pragma once
+
+#include "device_common.cuh"
+
+namespace scan {
+
+// Warp per vertex: number of lower neighbours and their total degree.
+__global__ void k_count_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                              uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    for (uint64_t v = warp; v < n; v += nwarps) {
+        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        uint32_t c = 0;
+        unsigned long long w = 0;
+        for (uint32_t j = b + lane; j < e; j += 32) {
+            const uint32_t u = adj[j];
+            const uint32_t du = off[u + 1] - off[u];
+            if (precedes(du, u, dv, (uint32_t)v)) { ++c; w += du; }
+        }
+        c = __reduce_add_sync(0xFFFFFFFFu, c);
+        for (int s = 16; s > 0; s >>= 1) w += __shfl_xor_sync(0xFFFFFFFFu, w, s);
+        if (lane == 0) { cnt[v] = c; work[v] = w; }
+    }
+}
+
+// Warp per vertex: write the lower neighbours of v at lo_off[v] in ascending id order.
+__global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                             const uint32_t* __restrict__ lo_off, uint32_t* __restrict__ lo_adj,
+                             uint32_t* __restrict__ lo_src) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint64_t v = warp; v < n; v += nwarps) {
+        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        uint32_t pos = lo_off[v];
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool low = false;
+            uint32_t u = 0;
+            if (j < e) {
+                u = adj[j];
+                low = precedes(off[u + 1] - off[u], u, dv, (uint32_t)v);
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
+            if (low) {
+                const uint32_t p = pos + __popc(mask & lt);
+                lo_adj[p] = u;
+                lo_src[p] = (uint32_t)v;
+            }
+            pos += __popc(mask);
+        }
+    }
+}
+
+// ---- exclusive scan of uint32 counts (n items) into out[0..n], out[n] = total ----------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* warp_sums, uint32_t* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = x;
+    for (int s = 1; s < 32; s <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+        if (lane >= s) incl += y;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        uint32_t ws = lane < nw ? warp_sums[lane] : 0;
+        uint32_t wi = ws;
+        for (int s = 1; s < 32; s <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, s);
+            if (lane >= s) wi += y;
+        }
+        if (lane < nw) warp_sums[lane] = wi - ws;
+        if (lane == nw - 1) *total = wi;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[wid] + incl - x;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in, uint64_t n,
+                                                             uint32_t* __restrict__ out, uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t t = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        v[i] = (base + i < n) ? in[base + i] : 0u;
+        t += v[i];
+    }
+    uint32_t ex = block_exclusive_scan(t, warp_sums, &total);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        if (base + i < n) out[base + i] = ex;
+        ex += v[i];
+    }
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of the tile sums in place; writes the grand total to *grand.
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t* __restrict__ sums, uint32_t ntiles,
+                                                            uint32_t* __restrict__ grand) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    uint32_t carry = 0;
+    for (uint32_t b0 = 0; b0 < ntiles; b0 += kScanThreads) {
+        const uint32_t i = b0 + threadIdx.x;
+        const uint32_t x = i < ntiles ? sums[i] : 0u;
+        const uint32_t ex = block_exclusive_scan(x, warp_sums, &total);
+        if (i < ntiles) sums[i] = carry + ex;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *grand = carry;
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_t* __restrict__ sums) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] += sums[i / kScanTile];
+}
+
+}  // namespace scan

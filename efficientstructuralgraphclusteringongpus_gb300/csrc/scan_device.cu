@@ -1,0 +1,601 @@
+// Device side of the engine: resident graph, orientation, task planning, the SCAN
+// pipeline and the C-ABI entry points that drive it.  One CUDA stream per resident graph;
+// every stage is timed with CUDA events on that stream.
+//
+// Pipeline (reference stages in GPUSCAN++/GPUScan.cu:800-1009 for comparison):
+//   upload     H2D of CSR, device-side input checks     (:836-851; checks of Graph.cpp:270-288)
+//   orient     lower-list construction                   (host getEidAndEdgeList, Graph.cpp:52-141)
+//   similarity cn for every edge (k_cn_small/k_cn_big)   (__check_core + lazy intersect, :276-367)
+//   predicate  eps test + similar-degree counts          (__prep_edge/__check_core, :133-172)
+//   cluster    cores, union-find, flatten                (__cluster_core1/2, __cluster_core, :479-652)
+//   attach     borders                                   (__cluster_noncore, :654-730)
+//   classify   hubs / outliers                           (__classify_others, :732-798)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "graph_internal.h"
+#include "kernels_cluster.cuh"
+#include "kernels_cn.cuh"
+#include "kernels_orient.cuh"
+
+namespace scan {
+
+#define SCAN_CUDA(call)                                                                               \
+    do {                                                                                              \
+        cudaError_t err_ = (call);                                                                    \
+        if (err_ != cudaSuccess)                                                                      \
+            return fail(SCAN_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));        \
+    } while (0)
+
+#define SCAN_TRY(expr)                        \
+    do {                                      \
+        scan_status st_ = (expr);             \
+        if (st_ != SCAN_OK) return st_;       \
+    } while (0)
+
+constexpr uint32_t kAdjPad = 8;   // zero entries past m so 16-byte loads never leave the array
+
+// Device-side input checks folded into the orientation count pass.
+constexpr uint32_t kBadId = 1u, kBadSelfLoop = 2u, kBadOrder = 4u, kBadOffsets = 8u;
+
+__global__ void k_offsets_from_u64(const uint64_t* __restrict__ in, uint64_t n1, uint32_t* __restrict__ out,
+                                   uint32_t* __restrict__ bad) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n1; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = in[i];
+        if (x > 0xFFFFFFFFull || (i > 0 && x < in[i - 1])) atomicOr(bad, kBadOffsets);
+        out[i] = (uint32_t)x;
+    }
+}
+
+__global__ void k_check_offsets32(const uint32_t* __restrict__ off, uint64_t n, uint64_t m, uint32_t* __restrict__ bad) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (off[i + 1] < off[i]) atomicOr(bad, kBadOffsets);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != m)) atomicOr(bad, kBadOffsets);
+}
+
+// Warp per vertex: ids in range, no self-loop, strictly ascending (the checks of
+// CheckInputGraph, GPUSCAN++/Graph.cpp:270-288, plus the id range it leaves unchecked).
+__global__ void k_check_lists(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                              uint32_t* __restrict__ bad) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    uint32_t flags = 0;
+    for (uint64_t v = warp; v < n; v += nwarps) {
+        const uint32_t b = off[v], e = off[v + 1];
+        for (uint32_t j = b + lane; j < e; j += 32) {
+            const uint32_t w = adj[j];
+            if (w >= n) flags |= kBadId;
+            if (w == (uint32_t)v) flags |= kBadSelfLoop;
+            if (j > b && w <= adj[j - 1]) flags |= kBadOrder;
+        }
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    if (flags && lane == 0) atomicOr(bad, flags);
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint64_t n, uint32_t x) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = x;
+}
+
+// Reference edge order (GPUSCAN++/Graph.cpp:87-111): edge {u lower, v higher} has id
+// P[u] + (rank of v among the higher neighbours of u), P = prefix of higher-neighbour
+// counts.  Used to return cn[] in the order the reference's Edge_u/Edge_v use.
+__global__ void k_higher_count(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ lo_off,
+                               uint32_t* __restrict__ hcnt) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        hcnt[v] = (off[v + 1] - off[v]) - (lo_off[v + 1] - lo_off[v]);
+}
+
+__global__ void k_to_reference_order(uint64_t E, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                                     const uint32_t* __restrict__ lo_off, const uint32_t* __restrict__ lo_adj,
+                                     const uint32_t* __restrict__ lo_src, const uint32_t* __restrict__ hpre,
+                                     const uint32_t* __restrict__ cn, uint32_t* __restrict__ out) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t u = lo_adj[e], v = lo_src[e];
+        const uint32_t pos = lower_bound_u32(adj, off[u], off[u + 1], v) - off[u];        // v's index in N(u)
+        const uint32_t lows = lower_bound_u32(lo_adj, lo_off[u], lo_off[u + 1], v) - lo_off[u];  // lower ones before v
+        out[hpre[u] + (pos - lows)] = cn[e];
+    }
+}
+
+}  // namespace scan
+
+using namespace scan;
+
+struct DeviceGraph {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0;
+    uint64_t m = 0, E = 0;
+    uint32_t* off = nullptr;
+    uint32_t* adj = nullptr;
+    uint32_t* lo_off = nullptr;
+    uint32_t* lo_adj = nullptr;
+    uint32_t* lo_src = nullptr;
+    unsigned long long* work = nullptr;
+    uint32_t* small_piv = nullptr;
+    uint32_t nsmall = 0;
+    CnTask* big[kNumBigClasses] = {};
+    uint32_t nbig[kNumBigClasses] = {};
+    uint32_t* cn = nullptr;
+    bool cn_valid = false;
+    // per-run scratch
+    uint8_t* sim = nullptr;
+    int32_t* sd = nullptr;
+    int32_t* parent = nullptr;
+    int32_t* bmin = nullptr;
+    int32_t* bmax = nullptr;
+    int32_t* nmin = nullptr;
+    int32_t* nmax = nullptr;
+    int32_t* lab = nullptr;
+    int32_t* label = nullptr;
+    uint8_t* role = nullptr;
+    RunCounters* ctr = nullptr;
+    uint32_t* scratch = nullptr;   // scan tile sums, flags, planner counters
+    std::vector<void*> allocs;
+    cudaEvent_t ev[10] = {};
+    std::mutex mu;                 // one run at a time per resident graph
+};
+
+namespace scan {
+
+void device_graph_free(DeviceGraph* d) {
+    if (!d) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (d->device >= 0) cudaSetDevice(d->device);
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    for (void* p : d->allocs) cudaFree(p);
+    for (auto& e : d->ev)
+        if (e) cudaEventDestroy(e);
+    if (d->stream) cudaStreamDestroy(d->stream);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete d;
+}
+
+template <typename T>
+static scan_status dalloc(DeviceGraph* d, T** p, uint64_t count) {
+    void* q = nullptr;
+    cudaError_t err = cudaMalloc(&q, std::max<uint64_t>(count, 1) * sizeof(T));
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SCAN_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(count * sizeof(T)) +
+                                                " bytes failed: " + cudaGetErrorString(err));
+    }
+    d->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return SCAN_OK;
+}
+
+static int grid_for(const DeviceGraph* d, uint64_t items, int threads, int per_sm = 8) {
+    uint64_t g = (items + threads - 1) / threads;
+    uint64_t cap = (uint64_t)d->num_sms * per_sm;
+    if (g > cap) g = cap;
+    return (int)std::max<uint64_t>(g, 1);
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// Exclusive scan of cnt[0..n) into out[0..n] on d->stream (out[n] = total).
+static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, uint32_t* out, uint32_t* sums) {
+    const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles > 0) {
+        k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, d->stream>>>(cnt, n, out, sums);
+        k_scan_sums<<<1, kScanThreads, 0, d->stream>>>(sums, (uint32_t)tiles, out + n);
+        k_scan_add<<<grid_for(d, n, 256), 256, 0, d->stream>>>(out, n, sums);
+    } else {
+        SCAN_CUDA(cudaMemsetAsync(out, 0, sizeof(uint32_t), d->stream));
+    }
+    SCAN_CUDA(cudaGetLastError());
+    return SCAN_OK;
+}
+
+// Upload a CSR (32- or 64-bit offsets) and build the lower lists and the task plan.
+static scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
+                                 const uint32_t* adj_host, DeviceGraph** out, scan_stats* st) {
+    if (n == 0 || n >= 0xFFFFFFFFull) return fail(SCAN_ERR_INVALID_ARG, "vertex count must be in [1, 2^32-1)");
+    if (m >= 0xFFFFFFF0ull) return fail(SCAN_ERR_TOO_LARGE, "m >= 2^32 directed entries");
+    SCAN_CUDA(cudaSetDevice(device));
+    std::unique_ptr<DeviceGraph, void (*)(DeviceGraph*)> d(new DeviceGraph(), device_graph_free);
+    d->device = device;
+    d->n = (uint32_t)n;
+    d->m = m;
+    SCAN_CUDA(cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, device));
+    SCAN_CUDA(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    for (auto& e : d->ev) SCAN_CUDA(cudaEventCreate(&e));
+    cudaStream_t s = d->stream;
+
+    SCAN_TRY(dalloc(d.get(), &d->off, n + 1));
+    SCAN_TRY(dalloc(d.get(), &d->adj, m + kAdjPad));
+    SCAN_TRY(dalloc(d.get(), &d->lo_off, n + 1));
+    SCAN_TRY(dalloc(d.get(), &d->work, n));
+    const uint64_t tiles = (n + 1 + kScanTile - 1) / kScanTile;
+    SCAN_TRY(dalloc(d.get(), &d->scratch, tiles + 64));
+    uint32_t* flags = d->scratch + tiles;        // [0] input checks, [1..4] planner counters
+    uint32_t* cnt = nullptr;
+    SCAN_TRY(dalloc(d.get(), &cnt, n));          // lower-neighbour counts (kept: reused below)
+
+    SCAN_CUDA(cudaEventRecord(d->ev[0], s));
+    SCAN_CUDA(cudaMemsetAsync(flags, 0, 64 * sizeof(uint32_t), s));
+    if (off64) {
+        uint64_t* tmp = nullptr;
+        SCAN_CUDA(cudaMalloc(&tmp, (n + 1) * sizeof(uint64_t)));
+        cudaError_t e1 = cudaMemcpyAsync(tmp, off_host, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+        if (e1 == cudaSuccess)
+            k_offsets_from_u64<<<grid_for(d.get(), n + 1, 256), 256, 0, s>>>(tmp, n + 1, d->off, flags);
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(tmp);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            return fail(SCAN_ERR_CUDA, std::string("offset upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    } else {
+        SCAN_CUDA(cudaMemcpyAsync(d->off, off_host, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    }
+    SCAN_CUDA(cudaMemcpyAsync(d->adj, adj_host, m * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    SCAN_CUDA(cudaMemsetAsync(d->adj + m, 0, kAdjPad * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaEventRecord(d->ev[1], s));
+
+    // Input checks first: the orientation kernels index by neighbour id.
+    k_check_offsets32<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->off, n, m, flags);
+    uint32_t bad = 0;
+    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    if (bad) return fail(SCAN_ERR_FORMAT, "offsets are not a non-decreasing sequence from 0 to m");
+    k_check_lists<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, flags);
+    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    if (bad & kBadId) return fail(SCAN_ERR_FORMAT, "neighbour id >= n");
+    if (bad & kBadSelfLoop) return fail(SCAN_ERR_FORMAT, "self loop");
+    if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
+
+    // Orientation.
+    k_count_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, cnt, d->work);
+    SCAN_TRY(device_scan(d.get(), cnt, n, d->lo_off, d->scratch));
+    uint32_t E32 = 0;
+    SCAN_CUDA(cudaMemcpyAsync(&E32, d->lo_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    d->E = E32;
+    if (d->E * 2 != m) return fail(SCAN_ERR_FORMAT, "graph is not symmetric (lower entries * 2 != m)");
+    SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
+    SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
+    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
+    SCAN_CUDA(cudaGetLastError());
+
+    // Task plan: count, size, fill.
+    PlanParams pp;
+    pp.target_probes = 1ull << 20;
+    pp.min_slice_edges = 64;
+    uint32_t* counts = flags + 1;
+    const unsigned pg = (unsigned)((n + 255) / 256);
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, pp, counts, nullptr, nullptr, nullptr, nullptr);
+    uint32_t hc[1 + kNumBigClasses];
+    SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    d->nsmall = hc[0];
+    SCAN_TRY(dalloc(d.get(), &d->small_piv, d->nsmall));
+    for (int c = 0; c < kNumBigClasses; ++c) {
+        d->nbig[c] = hc[1 + c];
+        SCAN_TRY(dalloc(d.get(), &d->big[c], d->nbig[c]));
+    }
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, pp, counts, d->small_piv, d->big[0], d->big[1],
+                              d->big[2]);
+    SCAN_CUDA(cudaGetLastError());
+
+    // Result and scratch arrays.
+    SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
+    SCAN_TRY(dalloc(d.get(), &d->sim, d->E));
+    SCAN_TRY(dalloc(d.get(), &d->sd, n));
+    SCAN_TRY(dalloc(d.get(), &d->parent, n));
+    SCAN_TRY(dalloc(d.get(), &d->bmin, n));
+    SCAN_TRY(dalloc(d.get(), &d->bmax, n));
+    SCAN_TRY(dalloc(d.get(), &d->nmin, n));
+    SCAN_TRY(dalloc(d.get(), &d->nmax, n));
+    SCAN_TRY(dalloc(d.get(), &d->lab, n));
+    SCAN_TRY(dalloc(d.get(), &d->label, n));
+    SCAN_TRY(dalloc(d.get(), &d->role, n));
+    SCAN_TRY(dalloc(d.get(), &d->ctr, 1));
+    SCAN_CUDA(cudaEventRecord(d->ev[2], s));
+    SCAN_CUDA(cudaEventSynchronize(d->ev[2]));
+    if (st) {
+        st->ms_h2d = ev_ms(d->ev[0], d->ev[1]);
+        st->ms_orient = ev_ms(d->ev[1], d->ev[2]);
+        st->kernel_launches += 10 + (off64 ? 1 : 0);
+    }
+    *out = d.release();
+    return SCAN_OK;
+}
+
+static bool g_attr_set[64] = {};
+
+// cn for every edge (the similarity stage).  Returns the number of kernels launched.
+static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
+    cudaStream_t s = d->stream;
+    SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
+    if (d->nsmall) {
+        constexpr int kWpb = 8;
+        k_cn_small<kWpb><<<grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16), kWpb * 32, 0, s>>>(
+            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn);
+        ++*launches;
+    }
+    if (d->device >= 0 && d->device < 64 && !g_attr_set[d->device]) {
+        SCAN_CUDA(cudaFuncSetAttribute(k_cn_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(big_class_slots(kNumBigClasses - 1) * sizeof(uint32_t))));
+        g_attr_set[d->device] = true;
+    }
+    for (int c = kNumBigClasses - 1; c >= 0; --c) {
+        if (!d->nbig[c]) continue;
+        const int threads = c == kNumBigClasses - 1 ? 512 : 256;
+        const size_t smem = big_class_slots(c) * sizeof(uint32_t);
+        int per_sm = 1;
+        SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
+        per_sm = std::max(per_sm, 1);
+        const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
+        k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off, d->adj,
+                                                        d->lo_adj, d->cn);
+        ++*launches;
+    }
+    SCAN_CUDA(cudaGetLastError());
+    return SCAN_OK;
+}
+
+// predicate -> cores -> union-find -> attach -> classify, on cached cn.
+static scan_status launch_cluster(DeviceGraph* d, const PredParams& pp, int mu, uint32_t* launches) {
+    cudaStream_t s = d->stream;
+    const uint64_t E = d->E;
+    const uint32_t n = d->n;
+    SCAN_CUDA(cudaMemsetAsync(d->sd, 0, n * sizeof(int32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(d->ctr, 0, sizeof(RunCounters), s));
+    const int T = 256;
+    k_predicate<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, d->sim, d->sd, d->ctr);
+    k_core_init<<<grid_for(d, n, T), T, 0, s>>>(n, d->sd, mu, d->parent, d->bmin, d->bmax, d->nmin, d->nmax);
+    k_union<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->ctr);
+    k_flatten<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent);
+    k_attach<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->bmin, d->bmax);
+    k_label<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->lab);
+    k_neighbour_labels<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->lab, d->nmin, d->nmax);
+    k_finalize<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->bmax, d->nmin, d->nmax, d->label, d->role,
+                                               d->ctr);
+    *launches += 8;
+    SCAN_CUDA(cudaGetLastError());
+    return SCAN_OK;
+}
+
+static scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode) {
+    if (!eps_decimal) return fail(SCAN_ERR_INVALID_ARG, "eps text is null");
+    uint64_t p = 0, q = 1;
+    double e = 0;
+    if (!parse_decimal(eps_decimal, &p, &q, &e))
+        return fail(SCAN_ERR_INVALID_ARG, std::string("cannot read eps from '") + eps_decimal + "'");
+    if (mode == SCAN_PRED_EXACT && p <= q && q > (1ull << 30))
+        return fail(SCAN_ERR_INVALID_ARG, "exact predicate: eps needs a denominator <= 2^30 (at most 9 decimals)");
+    if (mode != SCAN_PRED_EXACT && mode != SCAN_PRED_REF_F64) return fail(SCAN_ERR_INVALID_ARG, "unknown predicate");
+    pp->eps = e;
+    pp->p = p;
+    pp->q = q;
+    pp->mode = mode == SCAN_PRED_REF_F64 ? 1 : 0;
+    if (pp->p > pp->q) { pp->p = 1; pp->q = 0; }   // eps > 1: exact predicate is never true
+    return SCAN_OK;
+}
+
+static scan_status ensure_device(scan_graph* g, int device, scan_stats* st) {
+    if (device < 0) return fail(SCAN_ERR_INVALID_ARG, "device must be >= 0");
+    if (g->dev && g->dev->device == device) return SCAN_OK;
+    if (g->dev) { device_graph_free(g->dev); g->dev = nullptr; }
+    return device_upload(device, g->n, g->m, g->off.data(), true, g->adj.data(), &g->dev, st);
+}
+
+// Full run on a resident graph: cn (unless cached and reuse_cn), then the cluster stages,
+// then D2H of labels/roles.
+static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bool reuse_cn, int32_t* out_label,
+                                uint8_t* out_role, scan_stats* st) {
+    std::lock_guard<std::mutex> lock(d->mu);
+    SCAN_CUDA(cudaSetDevice(d->device));
+    cudaStream_t s = d->stream;
+    uint32_t launches = 0;
+    SCAN_CUDA(cudaEventRecord(d->ev[3], s));
+    if (!(reuse_cn && d->cn_valid)) SCAN_TRY(launch_cn(d, &launches));
+    SCAN_CUDA(cudaEventRecord(d->ev[4], s));
+    SCAN_TRY(launch_cluster(d, pp, mu, &launches));
+    SCAN_CUDA(cudaEventRecord(d->ev[5], s));
+    RunCounters hc;
+    if (out_label) SCAN_CUDA(cudaMemcpyAsync(out_label, d->label, d->n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (out_role) SCAN_CUDA(cudaMemcpyAsync(out_role, d->role, d->n, cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaMemcpyAsync(&hc, d->ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaEventRecord(d->ev[6], s));
+    SCAN_CUDA(cudaEventSynchronize(d->ev[6]));
+    d->cn_valid = true;
+    if (hc.error_flags) return fail(SCAN_ERR_DEVICE, "union-find exceeded its iteration limit");
+    if (st) {
+        st->n = d->n;
+        st->num_edges = d->E;
+        st->num_cores = hc.cores;
+        st->num_clusters = hc.clusters;
+        st->num_hubs = hc.hubs;
+        st->num_outliers = hc.outliers;
+        st->num_borders = hc.borders;
+        st->num_similar_edges = hc.similar_edges;
+        st->pred_disagreements = hc.disagreements;
+        st->multi_cluster_borders = hc.multi_borders;
+        st->ms_similarity = ev_ms(d->ev[3], d->ev[4]);
+        st->ms_cluster = ev_ms(d->ev[4], d->ev[5]);
+        st->ms_d2h = ev_ms(d->ev[5], d->ev[6]);
+        st->kernel_launches += launches;
+    }
+    return SCAN_OK;
+}
+
+}  // namespace scan
+
+extern "C" {
+
+scan_status scan_graph_upload(scan_graph* g, int device) {
+    clear_error();
+    if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
+    return ensure_device(g, device, nullptr);
+}
+
+scan_status scan_graph_release_device(scan_graph* g) {
+    clear_error();
+    if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
+    if (g->dev) { device_graph_free(g->dev); g->dev = nullptr; }
+    return SCAN_OK;
+}
+
+scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu, scan_predicate predicate,
+                     int32_t* out_label, uint8_t* out_role, scan_stats* stats) {
+    clear_error();
+    if (!g || !out_label) return fail(SCAN_ERR_INVALID_ARG, "graph and out_label must be non-null");
+    if (mu < 1) return fail(SCAN_ERR_INVALID_ARG, "mu must be >= 1");
+    PredParams pp;
+    SCAN_TRY(make_pred(eps_decimal, &pp, predicate));
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    SCAN_TRY(ensure_device(g, device, stats));
+    return run_resident(g->dev, pp, mu, false, out_label, out_role, stats);
+}
+
+scan_status scan_common_neighbors(scan_graph* g, int device, uint32_t* out_cn, scan_stats* stats) {
+    clear_error();
+    if (!g || !out_cn) return fail(SCAN_ERR_INVALID_ARG, "graph and out_cn must be non-null");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    SCAN_TRY(ensure_device(g, device, stats));
+    DeviceGraph* d = g->dev;
+    std::lock_guard<std::mutex> lock(d->mu);
+    SCAN_CUDA(cudaSetDevice(d->device));
+    cudaStream_t s = d->stream;
+    uint32_t launches = 0;
+    SCAN_CUDA(cudaEventRecord(d->ev[3], s));
+    SCAN_TRY(launch_cn(d, &launches));
+    SCAN_CUDA(cudaEventRecord(d->ev[4], s));
+    d->cn_valid = true;
+    // Reorder to the reference's edge ids.
+    uint32_t *hcnt = nullptr, *hpre = nullptr, *sums = nullptr, *ref = nullptr;
+    SCAN_CUDA(cudaMallocAsync(&hcnt, d->n * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMallocAsync(&hpre, (d->n + 1) * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMallocAsync(&sums, ((d->n + kScanTile) / kScanTile + 1) * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMallocAsync(&ref, std::max<uint64_t>(d->E, 1) * sizeof(uint32_t), s));
+    k_higher_count<<<grid_for(d, d->n, 256), 256, 0, s>>>(d->n, d->off, d->lo_off, hcnt);
+    scan_status st = device_scan(d, hcnt, d->n, hpre, sums);
+    if (st == SCAN_OK) {
+        k_to_reference_order<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->off, d->adj, d->lo_off, d->lo_adj,
+                                                                    d->lo_src, hpre, d->cn, ref);
+        cudaMemcpyAsync(out_cn, ref, d->E * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    }
+    cudaFreeAsync(hcnt, s);
+    cudaFreeAsync(hpre, s);
+    cudaFreeAsync(sums, s);
+    cudaFreeAsync(ref, s);
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    SCAN_CUDA(cudaGetLastError());
+    if (st) return st;
+    if (stats) {
+        stats->n = d->n;
+        stats->num_edges = d->E;
+        stats->ms_similarity = ev_ms(d->ev[3], d->ev[4]);
+        stats->kernel_launches += launches + 5;
+    }
+    return SCAN_OK;
+}
+
+scan_status scan_memberships(scan_graph* g, int device, const char* eps_decimal, int mu, scan_predicate predicate,
+                             int32_t* out_cluster, int32_t* out_vertex, uint64_t capacity, uint64_t* num_pairs) {
+    clear_error();
+    if (!g || !num_pairs) return fail(SCAN_ERR_INVALID_ARG, "graph and num_pairs must be non-null");
+    if (mu < 1) return fail(SCAN_ERR_INVALID_ARG, "mu must be >= 1");
+    PredParams pp;
+    SCAN_TRY(make_pred(eps_decimal, &pp, predicate));
+    SCAN_TRY(ensure_device(g, device, nullptr));
+    DeviceGraph* d = g->dev;
+    std::vector<int32_t> label(d->n);
+    std::vector<uint8_t> role(d->n);
+    SCAN_TRY(run_resident(d, pp, mu, true, label.data(), role.data(), nullptr));
+    std::lock_guard<std::mutex> lock(d->mu);
+    cudaStream_t s = d->stream;
+    // Border pairs: count, then collect.
+    unsigned long long* cnt = nullptr;
+    SCAN_CUDA(cudaMallocAsync(&cnt, sizeof(unsigned long long), s));
+    SCAN_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+    k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->sim, d->parent, cnt, nullptr, 0);
+    unsigned long long nb = 0;
+    SCAN_CUDA(cudaMemcpyAsync(&nb, cnt, sizeof(nb), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    std::vector<unsigned long long> keys(nb);
+    if (nb) {
+        unsigned long long* buf = nullptr;
+        SCAN_CUDA(cudaMallocAsync(&buf, nb * sizeof(unsigned long long), s));
+        SCAN_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+        k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->sim, d->parent, cnt, buf, nb);
+        SCAN_CUDA(cudaMemcpyAsync(keys.data(), buf, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        SCAN_CUDA(cudaFreeAsync(buf, s));
+    }
+    SCAN_CUDA(cudaFreeAsync(cnt, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    // Output formatting: add the cores, order by (cluster, vertex), drop repeats.
+    for (uint32_t v = 0; v < d->n; ++v)
+        if (role[v] == SCAN_ROLE_CORE) keys.push_back(((unsigned long long)(uint32_t)label[v] << 32) | v);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    *num_pairs = keys.size();
+    if (keys.size() > capacity || (!keys.empty() && (!out_cluster || !out_vertex)))
+        return fail(SCAN_ERR_INVALID_ARG, "capacity too small for " + std::to_string(keys.size()) + " pairs");
+    for (size_t i = 0; i < keys.size(); ++i) {
+        out_cluster[i] = (int32_t)(keys[i] >> 32);
+        out_vertex[i] = (int32_t)(uint32_t)keys[i];
+    }
+    return SCAN_OK;
+}
+
+int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj, const uint32_t* num_edges, const uint32_t* eid,
+                             const int32_t* edge_u, const int32_t* edge_v, double eps, int mu) {
+    (void)eid;
+    (void)edge_u;
+    (void)edge_v;
+    clear_error();
+    if (n <= 0 || m < 0 || !num_edges || (!adj && m > 0)) {
+        fail(SCAN_ERR_INVALID_ARG, "bad graph_t");
+        return nullptr;
+    }
+    if (mu < 1) {
+        fail(SCAN_ERR_INVALID_ARG, "mu must be >= 1");
+        return nullptr;
+    }
+    char text[48];
+    if (scan_eps_to_decimal(eps, text, sizeof(text)) != SCAN_OK) return nullptr;
+    PredParams pp;
+    if (make_pred(text, &pp, SCAN_PRED_REF_F64) != SCAN_OK) return nullptr;
+    pp.eps = eps;   // the double itself, exactly as the caller computed it
+    DeviceGraph* d = nullptr;
+    if (device_upload(0, (uint64_t)n, (uint64_t)m, num_edges, false, reinterpret_cast<const uint32_t*>(adj), &d,
+                      nullptr) != SCAN_OK)
+        return nullptr;
+    int32_t* out = static_cast<int32_t*>(std::malloc((size_t)n * sizeof(int32_t)));
+    if (!out) {
+        device_graph_free(d);
+        fail(SCAN_ERR_OUT_OF_MEMORY, "malloc of the result failed");
+        return nullptr;
+    }
+    scan_status st = run_resident(d, pp, mu, false, out, nullptr, nullptr);
+    device_graph_free(d);
+    if (st != SCAN_OK) {
+        std::free(out);
+        return nullptr;
+    }
+    return out;
+}
+
+}  // extern "C"

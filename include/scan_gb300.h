@@ -1,0 +1,187 @@
+/*
+ * scan_gb300.h -- C-ABI of the GB300-native SCAN structural graph clustering engine.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns a
+ * scan_status (never calls exit()), and records a message for scan_last_error().
+ *
+ * Reference interfaces replaced (paths are inside the GPUSCAN++ project):
+ *   Graph::Graph(char*)            GPUSCAN++/Graph.cpp:147-153   -> scan_graph_load
+ *   Graph::ReadDegree/ReadAdj...   GPUSCAN++/Graph.cpp:157-223   -> scan_graph_load
+ *   Graph::CheckInputGraph         GPUSCAN++/Graph.cpp:270-288   -> scan_graph_validate
+ *   getEidAndEdgeList              GPUSCAN++/Graph.cpp:52-141    -> scan_orient_reference
+ *   GPUScan(graph_t*,int*,int*,double,int)
+ *                                  GPUSCAN++/GPUScan.h:7,
+ *                                  GPUSCAN++/GPUScan.cu:800-1009 -> scan_run / scan_gpuscan_compat
+ *                                                                   (and the C++-linkage GPUScan
+ *                                                                   symbol in gpuscan_compat.h)
+ *   main's cluster count           GPUSCAN++/main.cpp:83-111     -> scan_count_clusters
+ *   csr_convert output format      csr_convert/EdgeListToBinsConverter.cpp:85-121
+ *                                                                -> scan_graph_save
+ *
+ * Output encoding of label[] follows the reference's role array (GPUSCAN++/GPUScan.cu:124-127,
+ * 780, 986): label >= 0 is a cluster id (the smallest core id of the cluster), -1 a hub,
+ * -2 an outlier.  role[] adds what the reference array cannot show: core vs border.
+ */
+#ifndef SCAN_GB300_H
+#define SCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum scan_status {
+    SCAN_OK = 0,
+    SCAN_ERR_INVALID_ARG = 1,   /* null pointer, eps/mu out of range, bad option            */
+    SCAN_ERR_IO = 2,            /* file missing, short read, write failure                  */
+    SCAN_ERR_FORMAT = 3,        /* header/size mismatch, self-loop, unsorted or duplicate    */
+    SCAN_ERR_CUDA = 4,          /* a CUDA runtime call failed                                */
+    SCAN_ERR_OUT_OF_MEMORY = 5, /* host or device allocation failed, or over the budget      */
+    SCAN_ERR_TOO_LARGE = 6,     /* graph exceeds the engine's index width (m >= 2^32)        */
+    SCAN_ERR_DEVICE = 7         /* a device-side check failed (bounded wait ran out, etc.)   */
+} scan_status;
+
+/* epsilon-similarity predicate.
+ * SCAN_PRED_REF_F64 reproduces the reference's IEEE double expressions with their operand
+ * order (GPUSCAN++/GPUScan.cu:145, 156, 220-221), so results are bit-identical to it.
+ * SCAN_PRED_EXACT evaluates (cn+2)^2 * q^2 >= p^2 * (du+1) * (dv+1) in 128-bit integers,
+ * with eps = p/q read exactly from the decimal string. */
+typedef enum scan_predicate {
+    SCAN_PRED_EXACT = 0,
+    SCAN_PRED_REF_F64 = 1
+} scan_predicate;
+
+/* Per-vertex role (out_role).  Core and border both carry a cluster id in label[]. */
+typedef enum scan_role {
+    SCAN_ROLE_OUTLIER = 0,
+    SCAN_ROLE_HUB = 1,
+    SCAN_ROLE_BORDER = 2,
+    SCAN_ROLE_CORE = 3
+} scan_role;
+
+typedef struct scan_graph scan_graph;   /* host CSR, optionally resident on the device */
+
+/* Per-run statistics; every time is device time from CUDA events on the run's stream. */
+typedef struct scan_stats {
+    uint64_t n;                 /* vertices                                                  */
+    uint64_t num_edges;         /* undirected edges E (= m/2)                                */
+    uint64_t num_cores;
+    uint64_t num_clusters;
+    uint64_t num_hubs;
+    uint64_t num_outliers;
+    uint64_t num_borders;
+    uint64_t num_similar_edges; /* undirected edges with sigma >= eps                        */
+    uint64_t pred_disagreements;/* edges where the exact and ref-f64 predicates differ        */
+    uint64_t multi_cluster_borders; /* border vertices similar to cores of >= 2 clusters      */
+    double ms_h2d;              /* host->device copies (0 when the graph is already resident) */
+    double ms_orient;           /* lower-list construction                                    */
+    double ms_similarity;       /* common-neighbour counting + predicate (the hot kernel)     */
+    double ms_cluster;          /* core flags, union-find, attach, hub/outlier                */
+    double ms_d2h;              /* result copies                                              */
+    double ms_total;            /* first event to last event                                  */
+    uint32_t kernel_launches;   /* kernels this library launched for the run                  */
+    uint32_t reserved;
+} scan_stats;
+
+/* ---- errors ------------------------------------------------------------------------- */
+/* Message of the last failing call on this host thread ("" if none). */
+const char* scan_last_error(void);
+const char* scan_status_string(scan_status s);
+/* Library version as "major.minor.patch". */
+const char* scan_version(void);
+
+/* ---- graphs ------------------------------------------------------------------------- */
+/* Read <dir>/b_degree.bin and <dir>/b_adj.bin (format written by csr_convert; a header
+ * int_size of 8 selects the 64-bit extension with uint64 n and m), then validate them. */
+scan_status scan_graph_load(const char* dir, scan_graph** out);
+/* Write the graph in the same two-file format (int_size 4 when n and m fit 32 bits). */
+scan_status scan_graph_save(const scan_graph* g, const char* dir);
+/* Build from caller CSR arrays (offsets n+1 entries, adjacency m entries).  The arrays
+ * are copied.  The graph is validated (sorted strictly ascending, no self-loops, ids < n). */
+scan_status scan_graph_from_csr(const uint64_t* offsets, const uint32_t* adj,
+                                uint64_t n, uint64_t m, scan_graph** out);
+/* Same, with 32-bit offsets as in the reference's graph_t (GPUSCAN++/Graph.h:20-27). */
+scan_status scan_graph_from_csr32(const uint32_t* offsets, const uint32_t* adj,
+                                  uint64_t n, uint64_t m, scan_graph** out);
+void scan_graph_free(scan_graph* g);
+uint64_t scan_graph_num_vertices(const scan_graph* g);
+uint64_t scan_graph_num_directed(const scan_graph* g);      /* m = 2E */
+uint32_t scan_graph_max_degree(const scan_graph* g);
+/* Borrow the host CSR arrays (valid until scan_graph_free). */
+const uint64_t* scan_graph_offsets(const scan_graph* g);
+const uint32_t* scan_graph_adjacency(const scan_graph* g);
+/* Re-run the input checks of CheckInputGraph; check_symmetry adds an O(m log d) check. */
+scan_status scan_graph_validate(const scan_graph* g, int check_symmetry);
+
+/* Copy the CSR to device `device` and keep it there (plus the lower-list orientation),
+ * so later scan_run calls start with inputs resident in HBM. */
+scan_status scan_graph_upload(scan_graph* g, int device);
+/* Drop the device copy (the host copy stays). */
+scan_status scan_graph_release_device(scan_graph* g);
+
+/* ---- generators (deterministic for a seed on every platform) ------------------------ */
+/* R-MAT: 2^scale vertices, edge_factor*2^scale sampled pairs with quadrant probabilities
+ * a, b, c (d = 1-a-b-c); symmetrised, deduplicated, self-loops removed, lists sorted. */
+scan_status scan_gen_rmat(int scale, int edge_factor, double a, double b, double c,
+                          uint64_t seed, scan_graph** out);
+/* Chung-Lu: power-law expected degrees w_i ~ (i+1)^(-1/(exponent-1)), scaled to
+ * ~target_edges undirected edges and capped at max_degree. */
+scan_status scan_gen_chung_lu(uint64_t n, double exponent, uint64_t target_edges,
+                              uint64_t max_degree, uint64_t seed, scan_graph** out);
+/* Stochastic block model with `blocks` equal communities, edge probabilities p_in/p_out,
+ * scaled down so the expected average degree is at most max_avg_degree. */
+scan_status scan_gen_sbm(uint64_t n, uint32_t blocks, double p_in, double p_out,
+                         double max_avg_degree, uint64_t seed, scan_graph** out);
+
+/* ---- reference-compatible orientation ------------------------------------------------ */
+/* getEidAndEdgeList (GPUSCAN++/Graph.cpp:52-141): eid[m] gives both directions of an
+ * undirected edge the same id; edge_u[E]/edge_v[E] hold the lower/higher endpoint in
+ * (degree, id) order; ids are grouped by the lower endpoint. */
+scan_status scan_orient_reference(const scan_graph* g, uint32_t* eid, int32_t* edge_u,
+                                  int32_t* edge_v);
+
+/* ---- the SCAN pipeline ------------------------------------------------------------- */
+/* Run SCAN(eps, mu) on device `device` (the graph is uploaded first if it is not resident
+ * there).  eps_decimal is the decimal text of epsilon ("0.5"), mu >= 1.
+ * out_label[n]: cluster id (smallest core id of the cluster) / -1 hub / -2 outlier.
+ * out_role[n] (may be NULL): scan_role values.  stats (may be NULL).
+ * Border vertices similar to cores of several clusters get the smallest such cluster id
+ * (the reference keeps whichever write lands last, GPUSCAN++/GPUScan.cu:716,722). */
+scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
+                     scan_predicate predicate, int32_t* out_label, uint8_t* out_role,
+                     scan_stats* stats);
+
+/* Exact common-neighbour count of every undirected edge, in the reference's edge order
+ * (the eid / edge_u / edge_v order of scan_orient_reference): out_cn[E]. */
+scan_status scan_common_neighbors(scan_graph* g, int device, uint32_t* out_cn,
+                                  scan_stats* stats);
+
+/* Every (cluster, vertex) membership pair: cores once, borders once per cluster they are
+ * similar to.  Pairs are sorted by (cluster, vertex).  *num_pairs receives the count; if
+ * capacity is smaller, nothing is written past it and SCAN_ERR_INVALID_ARG is returned. */
+scan_status scan_memberships(scan_graph* g, int device, const char* eps_decimal, int mu,
+                             scan_predicate predicate, int32_t* out_cluster,
+                             int32_t* out_vertex, uint64_t capacity, uint64_t* num_pairs);
+
+/* Drop-in for GPUScan (GPUSCAN++/GPUScan.h:7): host CSR in, malloc'd int[n] out that the
+ * caller frees with free().  eid/edge_u/edge_v are accepted for signature parity and not
+ * read (the engine orients the graph on the device).  Uses the ref-f64 predicate on
+ * device 0.  Returns NULL on failure (see scan_last_error()). */
+int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj,
+                             const uint32_t* num_edges, const uint32_t* eid,
+                             const int32_t* edge_u, const int32_t* edge_v, double eps,
+                             int mu);
+
+/* Number of distinct labels >= 0, as printed by the reference CLI (main.cpp:83-111). */
+uint64_t scan_count_clusters(const int32_t* label, uint64_t n);
+
+/* Shortest decimal text that reads back as `eps` (so 0.4 -> "0.4"); buf >= 32 bytes. */
+scan_status scan_eps_to_decimal(double eps, char* buf, size_t buflen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCAN_GB300_H */

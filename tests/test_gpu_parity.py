@@ -1,0 +1,203 @@
+"""CUDA engine vs the oracle: bit-identical labels, roles, counts and common-neighbour counts.
+
+Every test calls the engine through the C-ABI (libscan_gb300.so via ctypes).
+"""
+import numpy as np
+import pytest
+
+import efficientstructuralgraphclusteringongpus_gb300 as sg
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+EXACT, REF = sg.PRED_EXACT, sg.PRED_REF_F64
+
+
+def assert_same_as_oracle(g, eps, mu, mode):
+    res = g.run(eps, mu, predicate=mode)
+    label, role, counts = oracle.scan(g.offsets(), g.adjacency(), eps, mu, mode)
+    bad = np.flatnonzero(res.label != label)
+    assert bad.size == 0, f"eps={eps} mu={mu} mode={mode}: {bad.size} labels differ, first at {bad[:5]}"
+    assert np.array_equal(res.role, role)
+    st = res.stats
+    assert st["num_cores"] == counts["cores"]
+    assert st["num_clusters"] == counts["clusters"]
+    assert st["num_borders"] == counts["borders"]
+    assert st["num_hubs"] == counts["hubs"]
+    assert st["num_outliers"] == counts["outliers"]
+    assert st["num_similar_edges"] == counts["similar_edges"]
+    assert st["pred_disagreements"] == counts["disagreements"]
+    assert st["multi_cluster_borders"] == counts["multi_borders"]
+    return res
+
+
+# ---- hand-built graphs ------------------------------------------------------------------
+def two_cliques_bridge():
+    a = [(i, j) for i in range(6) for j in range(i + 1, 6)]
+    b = [(i, j) for i in range(6, 12) for j in range(i + 1, 12)]
+    return sg.Graph.from_edges(14, a + b + [(5, 6), (12, 0), (12, 7), (13, 3)])
+
+
+def star():
+    return sg.Graph.from_edges(40, [(0, i) for i in range(1, 40)] + [(1, 2), (2, 3)])
+
+
+def border_two_clusters():
+    # cliques {0..4} and {6..10}; vertex 5 adjacent to 3,4 and 6,7 (similar to both)
+    a = [(i, j) for i in range(5) for j in range(i + 1, 5)]
+    b = [(i, j) for i in range(6, 11) for j in range(i + 1, 11)]
+    return sg.Graph.from_edges(12, a + b + [(5, 3), (5, 4), (5, 6), (5, 7), (11, 0), (11, 9)])
+
+
+def degree_four_ring():
+    # every vertex degree 4, triangle-free: cn = 0, du = dv = 4 -> the eps=0.4 boundary edge
+    n = 20
+    return sg.Graph.from_edges(n, [(i, (i + 1) % n) for i in range(n)] + [(i, (i + 5) % n) for i in range(n)])
+
+
+HAND = {"cliques": two_cliques_bridge, "star": star, "border2": border_two_clusters, "ring4": degree_four_ring}
+
+
+@pytest.mark.parametrize("name", sorted(HAND))
+@pytest.mark.parametrize("eps", ["0.2", "0.4", "0.5", "0.7", "0.9", "1.0"])
+@pytest.mark.parametrize("mu", [1, 2, 3, 5])
+@pytest.mark.parametrize("mode", [EXACT, REF])
+def test_hand_built(name, eps, mu, mode):
+    assert_same_as_oracle(HAND[name](), eps, mu, mode)
+
+
+def test_eps_boundary_modes_differ():
+    g = degree_four_ring()
+    ex = assert_same_as_oracle(g, "0.4", 2, EXACT)
+    rf = assert_same_as_oracle(g, "0.4", 2, REF)
+    # exact: 2^2 * 25 >= 4 * 25 holds on every edge; the reference's double says no
+    assert ex.stats["num_similar_edges"] == g.num_edges
+    assert rf.stats["num_similar_edges"] == 0
+    assert ex.stats["pred_disagreements"] == g.num_edges
+
+
+def test_border_in_two_clusters_takes_smallest():
+    g = border_two_clusters()
+    res = assert_same_as_oracle(g, "0.5", 3, EXACT)
+    assert res.role[5] == sg.ROLE_BORDER
+    assert res.stats["multi_cluster_borders"] >= 1
+    cl, vx = g.memberships("0.5", 3, EXACT)
+    ocl, ovx = oracle.memberships(g.offsets(), g.adjacency(), "0.5", 3, EXACT)
+    assert np.array_equal(cl, ocl) and np.array_equal(vx, ovx)
+    assert len(set(cl[vx == 5].tolist())) == 2
+    assert res.label[5] == min(cl[vx == 5])
+
+
+def test_isolated_and_empty_edges():
+    g = sg.Graph.from_edges(10, [(0, 1)])
+    res = assert_same_as_oracle(g, "0.5", 1, EXACT)
+    assert (res.label[2:] == -2).all()
+
+
+# ---- generated graphs -------------------------------------------------------------------
+@pytest.mark.parametrize("scale,seed", [(8, 1), (10, 2), (12, 3), (14, 4)])
+@pytest.mark.parametrize("eps", ["0.2", "0.4", "0.5", "0.6", "0.8"])
+@pytest.mark.parametrize("mu", [2, 5, 10])
+def test_rmat_both_modes(scale, seed, eps, mu):
+    g = sg.Graph.rmat(scale, 16, seed=seed)
+    assert_same_as_oracle(g, eps, mu, EXACT)
+    assert_same_as_oracle(g, eps, mu, REF)
+
+
+def test_rmat16_reference_config():
+    """R-MAT scale 16, edge factor 16, eps=0.5, mu=5 (the reference's CPU-runnable case)."""
+    g = sg.Graph.rmat(16, 16, seed=1)
+    assert_same_as_oracle(g, "0.5", 5, REF)
+    assert_same_as_oracle(g, "0.5", 5, EXACT)
+
+
+@pytest.mark.parametrize("make", [
+    lambda: sg.Graph.rmat(12, 16, seed=11),
+    lambda: sg.Graph.rmat(16, 16, seed=1),
+    lambda: sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5),   # hubs above the chunk size
+    lambda: sg.Graph.sbm(20000, 16, 0.1, 0.001, 64, seed=2),
+    lambda: star(),
+])
+def test_common_neighbors_exact(make):
+    g = make()
+    cn, st = g.common_neighbors()
+    ref = oracle.common_neighbors(g.offsets(), g.adjacency())
+    assert cn.shape == ref.shape
+    bad = np.flatnonzero(cn != ref)
+    assert bad.size == 0, f"{bad.size} edges differ"
+    assert st["ms_similarity"] > 0
+
+
+def test_chunked_hub_pipeline():
+    g = sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5)
+    assert g.max_degree > 12288
+    for eps in ("0.1", "0.3"):
+        assert_same_as_oracle(g, eps, 3, EXACT)
+        assert_same_as_oracle(g, eps, 3, REF)
+
+
+def test_sbm_pipeline():
+    g = sg.Graph.sbm(5000, 8, 0.1, 0.001, 64, seed=3)
+    for eps in ("0.3", "0.5", "0.7"):
+        for mu in (2, 5, 8):
+            assert_same_as_oracle(g, eps, mu, EXACT)
+
+
+# ---- drop-in surfaces ----------------------------------------------------------------------
+def test_gpuscan_compat_matches_oracle():
+    g = sg.Graph.rmat(12, 16, seed=5)
+    off = g.offsets().astype(np.uint32)
+    adj = g.adjacency().astype(np.int32)
+    for eps, mu in ((0.5, 5), (0.4, 2), (0.8, 3)):
+        out = sg.GPUScan(off, adj, eps, mu)
+        label, _, _ = oracle.scan(g.offsets(), g.adjacency(), repr(eps), mu, REF)
+        assert np.array_equal(out, label)
+
+
+def test_repeat_runs_identical():
+    g = sg.Graph.rmat(13, 16, seed=9)
+    a = g.run("0.5", 5, EXACT)
+    b = g.run("0.5", 5, EXACT)
+    assert np.array_equal(a.label, b.label) and np.array_equal(a.role, b.role)
+
+
+def test_memberships_match_oracle():
+    g = sg.Graph.rmat(12, 16, seed=4)
+    for eps, mu in (("0.3", 3), ("0.5", 5)):
+        cl, vx = g.memberships(eps, mu, EXACT)
+        ocl, ovx = oracle.memberships(g.offsets(), g.adjacency(), eps, mu, EXACT)
+        assert np.array_equal(cl, ocl) and np.array_equal(vx, ovx)
+
+
+def test_cli_matches_library(tmp_path):
+    import subprocess
+
+    from efficientstructuralgraphclusteringongpus_gb300 import build
+
+    g = sg.Graph.rmat(11, 16, seed=6)
+    g.save(tmp_path / "g")
+    out = tmp_path / "labels.bin"
+    p = subprocess.run([str(build.CLI), str(tmp_path / "g"), "0.5", "5", "--out", str(out)], capture_output=True,
+                       text=True)
+    assert p.returncode == 0, p.stderr
+    lab = np.fromfile(out, dtype=np.int32)
+    label, _, _ = oracle.scan(g.offsets(), g.adjacency(), "0.5", 5, REF)
+    assert np.array_equal(lab, label)
+    assert f"Cluster Number: {sg.count_clusters(label)}" in p.stderr
+
+
+# ---- the reference's own kernels -----------------------------------------------------------
+@pytest.mark.parametrize("scale,seed,eps,mu", [(10, 1, "0.5", 5), (12, 2, "0.4", 3), (12, 3, "0.6", 2),
+                                               (14, 4, "0.5", 5), (16, 1, "0.5", 5)])
+def test_reference_kernels_admissible(scale, seed, eps, mu):
+    """The reference's GPU output must be one the oracle admits (cores and core clusters
+    identical; each border label one of the oracle's memberships; hub rule consistent)."""
+    if not oracle.reference_kernels_available():
+        pytest.skip("reference cubin not built (reference sources absent where build() ran)")
+    g = sg.Graph.rmat(scale, 16, seed=seed)
+    ref, _ = oracle.reference_gpuscan(g.offsets(), g.adjacency(), float(eps), mu)
+    viol = oracle.check_admissible(g.offsets(), g.adjacency(), eps, mu, REF, ref)
+    assert viol == {"core": 0, "border": 0, "membership": 0, "hub_rule": 0}, viol
+    # and our engine's answer is admissible in the same sense
+    res = g.run(eps, mu, REF)
+    assert oracle.check_admissible(g.offsets(), g.adjacency(), eps, mu, REF, res.label) == viol
