@@ -131,6 +131,7 @@ struct DeviceGraph {
     uint32_t nbig[kNumBigClasses] = {};
     uint32_t* cn = nullptr;
     bool cn_valid = false;
+    bool cn_valid_before = false;
     // per-run scratch
     uint8_t* sim = nullptr;
     int32_t* sd = nullptr;
@@ -145,7 +146,7 @@ struct DeviceGraph {
     RunCounters* ctr = nullptr;
     uint32_t* scratch = nullptr;   // scan tile sums, flags, planner counters
     std::vector<void*> allocs;
-    cudaEvent_t ev[10] = {};
+    cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-11 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
 };
 
@@ -323,35 +324,46 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
 
 static bool g_attr_set[64] = {};
 
-// cn for every edge (the similarity stage).  Returns the number of kernels launched.
+// cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
 static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
     cudaStream_t s = d->stream;
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaEventRecord(d->ev[7], s));
     if (d->nsmall) {
         constexpr int kWpb = 8;
         k_cn_small<kWpb><<<grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16), kWpb * 32, 0, s>>>(
             d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn);
         ++*launches;
     }
+    SCAN_CUDA(cudaEventRecord(d->ev[8], s));
     if (d->device >= 0 && d->device < 64 && !g_attr_set[d->device]) {
         SCAN_CUDA(cudaFuncSetAttribute(k_cn_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(big_class_slots(kNumBigClasses - 1) * sizeof(uint32_t))));
         g_attr_set[d->device] = true;
     }
-    for (int c = kNumBigClasses - 1; c >= 0; --c) {
-        if (!d->nbig[c]) continue;
-        const int threads = c == kNumBigClasses - 1 ? 512 : 256;
-        const size_t smem = big_class_slots(c) * sizeof(uint32_t);
-        int per_sm = 1;
-        SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
-        per_sm = std::max(per_sm, 1);
-        const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-        k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off, d->adj,
-                                                        d->lo_adj, d->cn);
-        ++*launches;
+    for (int c = 0; c < kNumBigClasses; ++c) {
+        if (d->nbig[c]) {
+            const int threads = c == kNumBigClasses - 1 ? 512 : 256;
+            const size_t smem = big_class_slots(c) * sizeof(uint32_t);
+            int per_sm = 1;
+            SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
+            per_sm = std::max(per_sm, 1);
+            const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
+            k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off,
+                                                            d->adj, d->lo_adj, d->cn);
+            ++*launches;
+        }
+        SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
     }
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
+}
+
+static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
+    st->ms_cn_kernel[0] = ev_ms(d->ev[7], d->ev[8]);
+    for (int c = 0; c < kNumBigClasses; ++c) st->ms_cn_kernel[1 + c] = ev_ms(d->ev[8 + c], d->ev[9 + c]);
+    st->cn_work_items[0] = d->nsmall;
+    for (int c = 0; c < kNumBigClasses; ++c) st->cn_work_items[1 + c] = d->nbig[c];
 }
 
 // predicate -> cores -> union-find -> attach -> classify, on cached cn.
@@ -409,6 +421,7 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
     cudaStream_t s = d->stream;
     uint32_t launches = 0;
     SCAN_CUDA(cudaEventRecord(d->ev[3], s));
+    d->cn_valid_before = d->cn_valid;
     if (!(reuse_cn && d->cn_valid)) SCAN_TRY(launch_cn(d, &launches));
     SCAN_CUDA(cudaEventRecord(d->ev[4], s));
     SCAN_TRY(launch_cluster(d, pp, mu, &launches));
@@ -435,6 +448,8 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
         st->ms_similarity = ev_ms(d->ev[3], d->ev[4]);
         st->ms_cluster = ev_ms(d->ev[4], d->ev[5]);
         st->ms_d2h = ev_ms(d->ev[5], d->ev[6]);
+        st->ms_total = ev_ms(d->ev[3], d->ev[6]);
+        if (!(reuse_cn && d->cn_valid_before)) cn_kernel_times(d, st);
         st->kernel_launches += launches;
     }
     return SCAN_OK;
@@ -507,6 +522,7 @@ scan_status scan_common_neighbors(scan_graph* g, int device, uint32_t* out_cn, s
         stats->n = d->n;
         stats->num_edges = d->E;
         stats->ms_similarity = ev_ms(d->ev[3], d->ev[4]);
+        cn_kernel_times(d, stats);
         stats->kernel_launches += launches + 5;
     }
     return SCAN_OK;

@@ -43,10 +43,11 @@ def star():
 
 
 def border_two_clusters():
-    # cliques {0..4} and {6..10}; vertex 5 adjacent to 3,4 and 6,7 (similar to both)
-    a = [(i, j) for i in range(5) for j in range(i + 1, 5)]
-    b = [(i, j) for i in range(6, 11) for j in range(i + 1, 11)]
-    return sg.Graph.from_edges(12, a + b + [(5, 3), (5, 4), (5, 6), (5, 7), (11, 0), (11, 9)])
+    # 7-cliques {0..6} and {8..14}; vertex 7 touches 5,6 and 8,9, vertex 15 touches 0 and 14.
+    # At eps=0.4, mu=5 both are non-cores similar to cores of both cliques.
+    a = [(i, j) for i in range(7) for j in range(i + 1, 7)]
+    b = [(i, j) for i in range(8, 15) for j in range(i + 1, 15)]
+    return sg.Graph.from_edges(16, a + b + [(7, 5), (7, 6), (7, 8), (7, 9), (15, 0), (15, 14)])
 
 
 def degree_four_ring():
@@ -78,14 +79,14 @@ def test_eps_boundary_modes_differ():
 
 def test_border_in_two_clusters_takes_smallest():
     g = border_two_clusters()
-    res = assert_same_as_oracle(g, "0.5", 3, EXACT)
-    assert res.role[5] == sg.ROLE_BORDER
-    assert res.stats["multi_cluster_borders"] >= 1
-    cl, vx = g.memberships("0.5", 3, EXACT)
-    ocl, ovx = oracle.memberships(g.offsets(), g.adjacency(), "0.5", 3, EXACT)
+    res = assert_same_as_oracle(g, "0.4", 5, EXACT)
+    assert (res.role[[7, 15]] == sg.ROLE_BORDER).all()
+    assert res.stats["num_clusters"] == 2 and res.stats["multi_cluster_borders"] == 2
+    cl, vx = g.memberships("0.4", 5, EXACT)
+    ocl, ovx = oracle.memberships(g.offsets(), g.adjacency(), "0.4", 5, EXACT)
     assert np.array_equal(cl, ocl) and np.array_equal(vx, ovx)
-    assert len(set(cl[vx == 5].tolist())) == 2
-    assert res.label[5] == min(cl[vx == 5])
+    assert sorted(cl[vx == 7].tolist()) == [0, 8]
+    assert res.label[7] == 0 and res.label[15] == 0
 
 
 def test_isolated_and_empty_edges():
