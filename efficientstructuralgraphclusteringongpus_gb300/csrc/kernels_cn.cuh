@@ -5,7 +5,7 @@
 // the link and attach phases (:579-584, :701-706).  Here every edge is counted exactly
 // once, grouped by its higher endpoint v (the pivot):
 //   1. the pivot's list N(v) (or one id-range chunk of it) is inserted into an
-//      open-addressing hash table in shared memory (load factor <= 1/2);
+//      open-addressing hash table in shared memory (load factor <= 1/4);
 //   2. warps stream the lower endpoints' lists N(u) with 16-byte loads and probe each
 //      element against the table; a warp reduction gives the count.
 // Per edge this reads deg(u) <= deg(v) entries, the shorter list, once; the longer
@@ -24,10 +24,10 @@ namespace scan {
 
 constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single warp
 constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
-constexpr uint32_t kChunkMax = 12288;      // max pivot entries staged by one CTA
+constexpr uint32_t kChunkMax = 6144;       // max pivot entries staged by one CTA
 constexpr int kNumBigClasses = 3;          // table capacities for chunk sizes below
 __host__ __device__ constexpr uint32_t big_class_entries(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : kChunkMax; }
-__host__ __device__ constexpr uint32_t big_class_slots(int c) { return 2u * big_class_entries(c); }
+__host__ __device__ constexpr uint32_t big_class_slots(int c) { return 4u * big_class_entries(c); }   // load <= 1/4
 
 struct CnTask {
     uint32_t v;      // pivot
@@ -39,7 +39,7 @@ struct CnTask {
     uint32_t pad0, pad1;
 };
 
-// Insert w into a table of `cap` slots (never full: load <= 1/2).
+// Insert w into a table of `cap` slots (never full: load <= 1/4).
 __device__ __forceinline__ void table_insert(uint32_t* tab, uint32_t cap, uint32_t w) {
     uint32_t s = hash_slot(w, cap);
     for (uint32_t it = 0; it < cap; ++it) {
@@ -58,21 +58,6 @@ __device__ __forceinline__ uint32_t table_has(const uint32_t* tab, uint32_t cap,
         s = (s + 1 == cap) ? 0 : s + 1;
     }
     return 0u;
-}
-
-// Count elements of adj[b, e) present in the table, 16-byte loads, one warp.
-// adj is padded by >= 4 entries past m and its base is 16-byte aligned.
-__device__ __forceinline__ uint32_t warp_probe_range(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
-                                                     const uint32_t* tab, uint32_t cap, uint32_t lane) {
-    uint32_t c = 0;
-    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128) {
-        const uint4 x = __ldg(reinterpret_cast<const uint4*>(adj + p));
-        if (p >= b) c += table_has(tab, cap, x.x);
-        if (p + 1 >= b && p + 1 < e) c += table_has(tab, cap, x.y);
-        if (p + 2 >= b && p + 2 < e) c += table_has(tab, cap, x.z);
-        if (p + 3 >= b && p + 3 < e) c += table_has(tab, cap, x.w);
-    }
-    return c;
 }
 
 // First position in adj[b, e) whose value is >= key (scalar, uniform across the warp).
@@ -117,31 +102,112 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
 }
 
 // Larger pivots: one CTA per task; table of `cap` slots in dynamic shared memory.
+//
+// Warps fetch batches of 32 edges from a shared counter.  Lane i loads edge i's list
+// bounds (narrowed to the task's id chunk when the pivot is split), so the dependent
+// loads of 32 edges overlap.  The batch's 32 lists, each widened to 16-byte boundaries,
+// form one stream of uint4 words; every round each lane takes one word (a binary search
+// over the batch's prefix sums names its list), loads it, and probes its valid entries.
+// All lanes stay busy whatever the list lengths.  Each edge's owner lane then adds the
+// hits that fell in its list from three ballots of the per-lane hit counts (0..4).
+constexpr int kRoundsPerStep = 2;   // words in flight per lane
+
+__device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
+    if (hi <= lo) return 0u;
+    const uint32_t upto = hi >= 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u);
+    return upto & ~((1u << lo) - 1u);
+}
+
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
     extern __shared__ uint32_t tab[];
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ uint32_t next_batch;
+    const uint32_t lane = threadIdx.x & 31;
     for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
         const CnTask tk = tasks[t];
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) tab[i] = kEmpty;
+        if (threadIdx.x == 0) next_batch = 0;
         __syncthreads();
         for (uint32_t j = tk.cb + threadIdx.x; j < tk.ce; j += blockDim.x) table_insert(tab, cap, adj[j]);
         __syncthreads();
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
         const uint32_t lo_id = (tk.cb > vb) ? adj[tk.cb] : 0u;          // chunk id range
         const uint32_t hi_id = (tk.ce < ve) ? adj[tk.ce - 1] : kEmpty;
-        for (uint32_t k = tk.e0 + wib; k < tk.e1; k += nw) {
-            const uint32_t u = lo_adj[k];
-            uint32_t ub = off[u], ue = off[u + 1];
-            if (tk.chunked) {
-                if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
-                if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
+        for (;;) {
+            uint32_t bidx = 0;
+            if (lane == 0) bidx = atomicAdd(&next_batch, 1u);
+            const uint32_t kb = tk.e0 + 32u * __shfl_sync(0xFFFFFFFFu, bidx, 0);
+            if (kb >= tk.e1) break;
+            const uint32_t k = kb + lane;
+            const bool valid = k < tk.e1;
+            uint32_t ub = 0, ue = 0;
+            if (valid) {
+                const uint32_t u = lo_adj[k];
+                ub = off[u];
+                ue = off[u + 1];
+                if (tk.chunked) {
+                    if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
+                    if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
+                }
             }
-            uint32_t c = warp_probe_range(adj, ub, ue, tab, cap, lane);
-            c = __reduce_add_sync(0xFFFFFFFFu, c);
-            if (lane == 0) {
-                if (tk.chunked) atomicAdd(&cn[k], c); else cn[k] = c;
+            const uint32_t wa = ub & ~3u;                                 // first word (entry index)
+            const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
+            uint32_t incl = nwords;
+#pragma unroll
+            for (int s = 1; s < 32; s <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+                if ((int)lane >= s) incl += y;
+            }
+            const uint32_t excl = incl - nwords;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            uint32_t cnt = 0;
+            for (uint32_t base = 0; base < total; base += 32 * kRoundsPerStep) {
+                uint32_t h[kRoundsPerStep];
+                uint4 x[kRoundsPerStep];
+                uint32_t pos[kRoundsPerStep], lb[kRoundsPerStep], le[kRoundsPerStep];
+#pragma unroll
+                for (int r = 0; r < kRoundsPerStep; ++r) {
+                    const uint32_t y = base + 32u * r + lane;
+                    uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
+#pragma unroll
+                    for (int s = 16; s > 0; s >>= 1) {
+                        const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
+                        if (pj <= y) j += s;
+                    }
+                    j &= 31u;
+                    const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
+                    const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
+                    lb[r] = __shfl_sync(0xFFFFFFFFu, ub, j);
+                    le[r] = __shfl_sync(0xFFFFFFFFu, ue, j);
+                    pos[r] = aj + 4u * (y - ej);
+                    x[r] = y < total ? __ldg(reinterpret_cast<const uint4*>(adj + pos[r])) : make_uint4(0, 0, 0, 0);
+                    if (y >= total) { lb[r] = 1; le[r] = 0; }
+                }
+#pragma unroll
+                for (int r = 0; r < kRoundsPerStep; ++r) {
+                    const uint32_t p = pos[r];
+                    uint32_t c = 0;
+                    if (p >= lb[r] && p < le[r]) c += table_has(tab, cap, x[r].x);
+                    if (p + 1 >= lb[r] && p + 1 < le[r]) c += table_has(tab, cap, x[r].y);
+                    if (p + 2 >= lb[r] && p + 2 < le[r]) c += table_has(tab, cap, x[r].z);
+                    if (p + 3 >= lb[r] && p + 3 < le[r]) c += table_has(tab, cap, x[r].w);
+                    h[r] = c;
+                }
+#pragma unroll
+                for (int r = 0; r < kRoundsPerStep; ++r) {
+                    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h[r] & 1u);
+                    const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h[r] & 2u);
+                    const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h[r] & 4u);
+                    const int64_t rb = (int64_t)base + 32 * r;
+                    const int lo = (int)min(max((int64_t)excl - rb, (int64_t)0), (int64_t)32);
+                    const int hi = (int)min(max((int64_t)incl - rb, (int64_t)0), (int64_t)32);
+                    const uint32_t m = lane_range_mask(lo, hi);
+                    cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+                }
+            }
+            if (valid) {
+                if (tk.chunked) atomicAdd(&cn[k], cnt); else cn[k] = cnt;
             }
         }
         __syncthreads();

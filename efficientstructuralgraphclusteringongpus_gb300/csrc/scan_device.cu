@@ -279,7 +279,7 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
 
     // Task plan: count, size, fill.
     PlanParams pp;
-    pp.target_probes = 1ull << 20;
+    pp.target_probes = 1ull << 22;
     pp.min_slice_edges = 64;
     uint32_t* counts = flags + 1;
     const unsigned pg = (unsigned)((n + 255) / 256);
@@ -343,7 +343,7 @@ static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
     }
     for (int c = 0; c < kNumBigClasses; ++c) {
         if (d->nbig[c]) {
-            const int threads = c == kNumBigClasses - 1 ? 512 : 256;
+            const int threads = c == 0 ? 256 : 512;
             const size_t smem = big_class_slots(c) * sizeof(uint32_t);
             int per_sm = 1;
             SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));

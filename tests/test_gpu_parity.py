@@ -50,6 +50,11 @@ def border_two_clusters():
     return sg.Graph.from_edges(16, a + b + [(7, 5), (7, 6), (7, 8), (7, 9), (15, 0), (15, 14)])
 
 
+def wheel(spokes):
+    rim = [(i, i % spokes + 1) for i in range(1, spokes + 1)]
+    return sg.Graph.from_edges(spokes + 1, [(0, i) for i in range(1, spokes + 1)] + rim)
+
+
 def degree_four_ring():
     # every vertex degree 4, triangle-free: cn = 0, du = dv = 4 -> the eps=0.4 boundary edge
     n = 20
@@ -116,8 +121,10 @@ def test_rmat16_reference_config():
     lambda: sg.Graph.rmat(12, 16, seed=11),
     lambda: sg.Graph.rmat(16, 16, seed=1),
     lambda: sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5),   # hubs above the chunk size
+    lambda: sg.Graph.chung_lu(200000, 2.1, 1500000, 60000, seed=8),
     lambda: sg.Graph.sbm(20000, 16, 0.1, 0.001, 64, seed=2),
     lambda: star(),
+    lambda: wheel(20000),                                            # one pivot in several chunks
 ])
 def test_common_neighbors_exact(make):
     g = make()
@@ -129,9 +136,15 @@ def test_common_neighbors_exact(make):
     assert st["ms_similarity"] > 0
 
 
+def test_wheel_hub_pipeline():
+    g = wheel(20000)
+    for eps in ("0.01", "0.3"):
+        assert_same_as_oracle(g, eps, 2, EXACT)
+
+
 def test_chunked_hub_pipeline():
     g = sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5)
-    assert g.max_degree > 12288
+    assert g.max_degree > 6144          # above the per-CTA chunk: the hub is split
     for eps in ("0.1", "0.3"):
         assert_same_as_oracle(g, eps, 3, EXACT)
         assert_same_as_oracle(g, eps, 3, REF)
