@@ -132,14 +132,24 @@ __global__ void k_union(uint64_t E, const uint32_t* __restrict__ lo_adj, const u
     }
 }
 
-__global__ void k_flatten(uint32_t n, int32_t* parent) {
+// Flatten by pointer jumping: parent[v] = parent[parent[v]] for every core, repeated by the
+// host until no pointer changes (O(log depth) rounds).  Every value stored is an ancestor of
+// v in the final forest, so concurrent jumps never undo one another; a find with path
+// halving here would not be safe, because its halving store can overwrite a vertex whose
+// root another thread has just written with an intermediate ancestor.
+__global__ void k_jump(uint32_t n, int32_t* parent, uint32_t* changed) {
     volatile int32_t* vp = parent;
+    uint32_t ch = 0;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        if (vp[v] >= 0) {
-            const int32_t r = uf_find(vp, (int32_t)v);
-            vp[v] = r;
+        const int32_t p = vp[v];
+        if (p < 0) continue;
+        const int32_t g = vp[p];
+        if (g != p) {
+            vp[v] = g;
+            ch = 1;
         }
     }
+    if (__any_sync(0xFFFFFFFFu, ch) && (threadIdx.x & 31) == 0) atomicOr(changed, 1u);
 }
 
 // Border attachment: a non-core similar to a core joins that core's cluster.  The

@@ -5,7 +5,8 @@
 // the link and attach phases (:579-584, :701-706).  Here every edge is counted exactly
 // once, grouped by its higher endpoint v (the pivot):
 //   1. the pivot's list N(v) (or one id-range chunk of it) is inserted into an
-//      open-addressing hash table in shared memory (load factor <= 1/4);
+//      open-addressing hash table in shared memory (load factor <= 1/4; the CTA-wide
+//      kernel uses 4-slot buckets read with one 16-byte load);
 //   2. warps stream the lower endpoints' lists N(u) with 16-byte loads and probe each
 //      element against the table; a warp reduction gives the count.
 // Per edge this reads deg(u) <= deg(v) entries, the shorter list, once; the longer
@@ -60,6 +61,36 @@ __device__ __forceinline__ uint32_t table_has(const uint32_t* tab, uint32_t cap,
     return 0u;
 }
 
+// Bucketed table for the CTA-wide kernel: buckets of 4 slots (one 16-byte shared load),
+// linear probing over buckets.  Insertion fills a bucket's slots in order, so a bucket
+// whose last slot is empty ends every probe sequence through it.
+__device__ __forceinline__ void bucket_insert(uint32_t* tab, uint32_t nb, uint32_t w) {
+    uint32_t b = hash_slot(w, nb);
+    for (uint32_t it = 0; it < nb; ++it) {
+        uint32_t* s = tab + 4 * b;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t old = atomicCAS(&s[i], kEmpty, w);
+            if (old == kEmpty || old == w) return;
+        }
+        b = (b + 1 == nb) ? 0 : b + 1;
+    }
+}
+
+__device__ __forceinline__ uint32_t bucket_has(const uint32_t* tab, uint32_t nb, uint32_t w) {
+    uint32_t b = hash_slot(w, nb);
+    uint4 q = *reinterpret_cast<const uint4*>(tab + 4 * b);
+    uint32_t hit = (q.x == w) | (q.y == w) | (q.z == w) | (q.w == w);
+    if (hit || q.w == kEmpty) return hit;
+    for (uint32_t it = 1; it < nb; ++it) {   // the home bucket is full: rare at load <= 1/4
+        b = (b + 1 == nb) ? 0 : b + 1;
+        q = *reinterpret_cast<const uint4*>(tab + 4 * b);
+        hit = (q.x == w) | (q.y == w) | (q.z == w) | (q.w == w);
+        if (hit || q.w == kEmpty) return hit;
+    }
+    return 0u;
+}
+
 // First position in adj[b, e) whose value is >= key (scalar, uniform across the warp).
 __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
                                                     uint32_t key) {
@@ -101,16 +132,20 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
     }
 }
 
-// Larger pivots: one CTA per task; table of `cap` slots in dynamic shared memory.
+// Larger pivots: one CTA per task; a bucketed table of `cap` slots (cap/4 buckets) in
+// dynamic shared memory.
 //
 // Warps fetch batches of 32 edges from a shared counter.  Lane i loads edge i's list
 // bounds (narrowed to the task's id chunk when the pivot is split), so the dependent
-// loads of 32 edges overlap.  The batch's 32 lists, each widened to 16-byte boundaries,
-// form one stream of uint4 words; every round each lane takes one word (a binary search
-// over the batch's prefix sums names its list), loads it, and probes its valid entries.
-// All lanes stay busy whatever the list lengths.  Each edge's owner lane then adds the
-// hits that fell in its list from three ballots of the per-lane hit counts (0..4).
-constexpr int kRoundsPerStep = 2;   // words in flight per lane
+// loads of 32 edges overlap.  Then
+//   * lists of at least kLongWords 16-byte words are streamed one at a time by the whole
+//     warp, two words in flight per lane, and counted with one warp reduction;
+//   * the shorter lists, each widened to 16-byte boundaries, form one stream of words;
+//     every round each lane takes one word (a binary search over the batch's prefix sums
+//     names its list), loads it and probes its valid entries, and each edge's owner lane
+//     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
+constexpr uint32_t kLongWords = 32;   // lists of >= 128 entries take the whole warp
+constexpr int kWordsInFlight = 2;
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
     if (hi <= lo) return 0u;
@@ -118,18 +153,47 @@ __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
     return upto & ~((1u << lo) - 1u);
 }
 
+__device__ __forceinline__ uint32_t probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
+                                               const uint32_t* tab, uint32_t nb) {
+    uint32_t c = 0;
+    if (p >= lb && p < le) c += bucket_has(tab, nb, x.x);
+    if (p + 1 >= lb && p + 1 < le) c += bucket_has(tab, nb, x.y);
+    if (p + 2 >= lb && p + 2 < le) c += bucket_has(tab, nb, x.z);
+    if (p + 3 >= lb && p + 3 < le) c += bucket_has(tab, nb, x.w);
+    return c;
+}
+
+// One list adj[b, e) streamed by the whole warp; returns this lane's hits.
+__device__ __forceinline__ uint32_t warp_probe_list(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
+                                                    const uint32_t* tab, uint32_t nb, uint32_t lane) {
+    uint32_t c = 0;
+    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
+        uint4 x[kWordsInFlight];
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) {
+            const uint32_t pq = p + 128 * q;
+            x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(adj + pq)) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) c += probe_word(x[q], p + 128 * q, b, e, tab, nb);
+    }
+    return c;
+}
+
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
-    extern __shared__ uint32_t tab[];
+    extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch;
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nb = cap / 4;
     for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
         const CnTask tk = tasks[t];
-        for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) tab[i] = kEmpty;
+        for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+            reinterpret_cast<uint4*>(tab)[i] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
         if (threadIdx.x == 0) next_batch = 0;
         __syncthreads();
-        for (uint32_t j = tk.cb + threadIdx.x; j < tk.ce; j += blockDim.x) table_insert(tab, cap, adj[j]);
+        for (uint32_t j = tk.cb + threadIdx.x; j < tk.ce; j += blockDim.x) bucket_insert(tab, nb, adj[j]);
         __syncthreads();
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
         const uint32_t lo_id = (tk.cb > vb) ? adj[tk.cb] : 0u;          // chunk id range
@@ -153,58 +217,51 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
             }
             const uint32_t wa = ub & ~3u;                                 // first word (entry index)
             const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
-            uint32_t incl = nwords;
+            uint32_t cnt = 0;
+            // long lists: the whole warp, one list at a time
+            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= kLongWords);
+            while (longs) {
+                const int j = __ffs(longs) - 1;
+                longs &= longs - 1;
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
+                const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, warp_probe_list(adj, b, e, tab, nb, lane));
+                if ((int)lane == j) cnt = c;
+            }
+            // short lists: one stream of words
+            const uint32_t sw = nwords < kLongWords ? nwords : 0u;
+            uint32_t incl = sw;
 #pragma unroll
             for (int s = 1; s < 32; s <<= 1) {
                 const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
                 if ((int)lane >= s) incl += y;
             }
-            const uint32_t excl = incl - nwords;
+            const uint32_t excl = incl - sw;
             const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            uint32_t cnt = 0;
-            for (uint32_t base = 0; base < total; base += 32 * kRoundsPerStep) {
-                uint32_t h[kRoundsPerStep];
-                uint4 x[kRoundsPerStep];
-                uint32_t pos[kRoundsPerStep], lb[kRoundsPerStep], le[kRoundsPerStep];
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t y = base + lane;
+                uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
 #pragma unroll
-                for (int r = 0; r < kRoundsPerStep; ++r) {
-                    const uint32_t y = base + 32u * r + lane;
-                    uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
-#pragma unroll
-                    for (int s = 16; s > 0; s >>= 1) {
-                        const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
-                        if (pj <= y) j += s;
-                    }
-                    j &= 31u;
-                    const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
-                    const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
-                    lb[r] = __shfl_sync(0xFFFFFFFFu, ub, j);
-                    le[r] = __shfl_sync(0xFFFFFFFFu, ue, j);
-                    pos[r] = aj + 4u * (y - ej);
-                    x[r] = y < total ? __ldg(reinterpret_cast<const uint4*>(adj + pos[r])) : make_uint4(0, 0, 0, 0);
-                    if (y >= total) { lb[r] = 1; le[r] = 0; }
+                for (int s = 16; s > 0; s >>= 1) {
+                    const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
+                    if (pj <= y) j += s;
                 }
-#pragma unroll
-                for (int r = 0; r < kRoundsPerStep; ++r) {
-                    const uint32_t p = pos[r];
-                    uint32_t c = 0;
-                    if (p >= lb[r] && p < le[r]) c += table_has(tab, cap, x[r].x);
-                    if (p + 1 >= lb[r] && p + 1 < le[r]) c += table_has(tab, cap, x[r].y);
-                    if (p + 2 >= lb[r] && p + 2 < le[r]) c += table_has(tab, cap, x[r].z);
-                    if (p + 3 >= lb[r] && p + 3 < le[r]) c += table_has(tab, cap, x[r].w);
-                    h[r] = c;
+                j &= 31u;
+                const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
+                const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
+                const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, j);
+                const uint32_t le = __shfl_sync(0xFFFFFFFFu, ue, j);
+                uint32_t h = 0;
+                if (y < total) {
+                    const uint32_t p = aj + 4u * (y - ej);
+                    h = probe_word(__ldg(reinterpret_cast<const uint4*>(adj + p)), p, lb, le, tab, nb);
                 }
-#pragma unroll
-                for (int r = 0; r < kRoundsPerStep; ++r) {
-                    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h[r] & 1u);
-                    const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h[r] & 2u);
-                    const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h[r] & 4u);
-                    const int64_t rb = (int64_t)base + 32 * r;
-                    const int lo = (int)min(max((int64_t)excl - rb, (int64_t)0), (int64_t)32);
-                    const int hi = (int)min(max((int64_t)incl - rb, (int64_t)0), (int64_t)32);
-                    const uint32_t m = lane_range_mask(lo, hi);
-                    cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
-                }
+                const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
+                const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
+                const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
+                const int lo = (int)min(max((int64_t)excl - (int64_t)base, (int64_t)0), (int64_t)32);
+                const int hi = (int)min(max((int64_t)incl - (int64_t)base, (int64_t)0), (int64_t)32);
+                const uint32_t m = lane_range_mask(lo, hi);
+                cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
             }
             if (valid) {
                 if (tk.chunked) atomicAdd(&cn[k], cnt); else cn[k] = cnt;

@@ -144,7 +144,8 @@ struct DeviceGraph {
     int32_t* label = nullptr;
     uint8_t* role = nullptr;
     RunCounters* ctr = nullptr;
-    uint32_t* scratch = nullptr;   // scan tile sums, flags, planner counters
+    uint32_t* scratch = nullptr;   // scan tile sums, then dflags
+    uint32_t* dflags = nullptr;    // [0] input checks, [1..4] planner counters, [8] flatten flag
     std::vector<void*> allocs;
     cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-11 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
@@ -229,6 +230,7 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     const uint64_t tiles = (n + 1 + kScanTile - 1) / kScanTile;
     SCAN_TRY(dalloc(d.get(), &d->scratch, tiles + 64));
     uint32_t* flags = d->scratch + tiles;        // [0] input checks, [1..4] planner counters
+    d->dflags = flags;
     uint32_t* cnt = nullptr;
     SCAN_TRY(dalloc(d.get(), &cnt, n));          // lower-neighbour counts (kept: reused below)
 
@@ -377,13 +379,26 @@ static scan_status launch_cluster(DeviceGraph* d, const PredParams& pp, int mu, 
     k_predicate<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, d->sim, d->sd, d->ctr);
     k_core_init<<<grid_for(d, n, T), T, 0, s>>>(n, d->sd, mu, d->parent, d->bmin, d->bmax, d->nmin, d->nmax);
     k_union<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->ctr);
-    k_flatten<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent);
+    *launches += 1;
+    // Flatten: two pointer-jumping rounds per check until nothing changes.
+    uint32_t* changed = d->dflags + 8;
+    for (int round = 0;; ++round) {
+        if (round >= 40) return fail(SCAN_ERR_DEVICE, "union-find flattening did not converge");
+        SCAN_CUDA(cudaMemsetAsync(changed, 0, sizeof(uint32_t), s));
+        k_jump<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, changed);
+        k_jump<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, changed);
+        *launches += 2;
+        uint32_t h = 0;
+        SCAN_CUDA(cudaMemcpyAsync(&h, changed, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        SCAN_CUDA(cudaStreamSynchronize(s));
+        if (!h) break;
+    }
     k_attach<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->bmin, d->bmax);
     k_label<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->lab);
     k_neighbour_labels<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->lab, d->nmin, d->nmax);
     k_finalize<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->bmax, d->nmin, d->nmax, d->label, d->role,
                                                d->ctr);
-    *launches += 8;
+    *launches += 6;
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }

@@ -142,6 +142,14 @@ def test_wheel_hub_pipeline():
         assert_same_as_oracle(g, eps, 2, EXACT)
 
 
+@pytest.mark.parametrize("n", [5000, 200000])
+def test_triangle_strip_one_long_cluster(n):
+    # every vertex is a core and the cluster is one long chain: deep union-find forests
+    g = sg.Graph.from_edges(n, [(i, i + 1) for i in range(n - 1)] + [(i, i + 2) for i in range(n - 2)])
+    res = assert_same_as_oracle(g, "0.3", 2, EXACT)
+    assert res.stats["num_clusters"] == 1 and (res.label == 0).all()
+
+
 def test_chunked_hub_pipeline():
     g = sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5)
     assert g.max_degree > 6144          # above the per-CTA chunk: the hub is split
