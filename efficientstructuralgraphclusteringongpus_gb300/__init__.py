@@ -49,7 +49,7 @@ class ScanStats(C.Structure):
         "n", "num_edges", "num_cores", "num_clusters", "num_hubs", "num_outliers", "num_borders",
         "num_similar_edges", "pred_disagreements", "multi_cluster_borders")] + [
         (name, C.c_double) for name in ("ms_h2d", "ms_orient", "ms_similarity", "ms_cluster", "ms_d2h", "ms_total")] + [
-        ("ms_cn_kernel", C.c_double * 4), ("cn_work_items", C.c_uint64 * 4),
+        ("ms_cn_kernel", C.c_double * 5), ("cn_work_items", C.c_uint64 * 5),
         ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
 
     def as_dict(self) -> dict:

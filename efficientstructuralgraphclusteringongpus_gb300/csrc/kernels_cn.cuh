@@ -27,6 +27,14 @@ constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single w
 constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
 constexpr uint32_t kChunkMax = 6144;       // max pivot entries staged by one CTA
 constexpr int kNumBigClasses = 3;          // table capacities for chunk sizes below
+// Bitmap path: the kHotBits highest-degree vertices get ids in [0, kHotBits) ("hot");
+// every other vertex x is kHotBits + x.  A pivot's hot neighbours go into a shared-memory
+// bitmap (one bit per hot id, 128 KB), the rest (its "tail") into a bucketed table.
+constexpr uint32_t kHotBits = 1u << 20;
+constexpr uint32_t kTailSlots = 24576;     // 96 KB; tails up to kTailMax entries (load <= 1/2)
+constexpr uint32_t kTailMax = kTailSlots / 2;
+constexpr uint32_t kBitmapMinDeg = 1024;   // pivots above this degree use the bitmap path
+constexpr int kBitmapThreads = 1024;
 __host__ __device__ constexpr uint32_t big_class_entries(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : kChunkMax; }
 __host__ __device__ constexpr uint32_t big_class_slots(int c) { return 4u * big_class_entries(c); }   // load <= 1/4
 
@@ -271,20 +279,161 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
     }
 }
 
-// Task planner.  Pass 1 (tasks == nullptr) counts tasks per class; pass 2 writes them.
-// counts[0] = small pivots, counts[1 + c] = tasks of big class c.
+// Bitmap path: one CTA of kBitmapThreads per task (pivot, edge slice), one CTA per SM.
+// Shared memory: the hot bitmap (zeroed once; each task sets its pivot's bits and clears
+// them again) and the tail table.  Probing an entry is one 4-byte shared load for hot ids.
+__device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
+                                                      const uint32_t* bits, const uint32_t* tail, uint32_t ntb) {
+    const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+    uint32_t c = 0, tails = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t pos = p + i;
+        if (pos >= lb && pos < le) {
+            if (w[i] < kHotBits) c += (bits[w[i] >> 5] >> (w[i] & 31u)) & 1u;
+            else tails |= 1u << i;
+        }
+    }
+    while (tails) {
+        const int i = __ffs(tails) - 1;
+        tails &= tails - 1;
+        c += bucket_has(tail, ntb, w[i]);
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint32_t warp_probe_list_bitmap(const uint32_t* __restrict__ radj, uint32_t b, uint32_t e,
+                                                           const uint32_t* bits, const uint32_t* tail, uint32_t ntb,
+                                                           uint32_t lane) {
+    uint32_t c = 0;
+    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
+        uint4 x[kWordsInFlight];
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) {
+            const uint32_t pq = p + 128 * q;
+            x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(radj + pq)) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) c += bitmap_probe_word(x[q], p + 128 * q, b, e, bits, tail, ntb);
+    }
+    return c;
+}
+
+// task.cb carries the pivot's tail size.
+__global__ void __launch_bounds__(kBitmapThreads, 1)
+k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ off,
+            const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* bits = smem;                              // kHotBits / 32 words
+    uint32_t* tail = smem + kHotBits / 32;              // kTailSlots words
+    __shared__ uint32_t next_batch;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < kHotBits / 128; i += blockDim.x)
+        reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const CnTask tk = tasks[t];
+        const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
+        uint32_t ntb = 8;                                // tail buckets: >= tail size (load <= 1/4),
+        while (ntb < tk.cb) ntb <<= 1;                   // capped at the table (load <= 1/2 there)
+        ntb = min(ntb, kTailSlots / 4);
+        for (uint32_t i = threadIdx.x; i < ntb; i += blockDim.x)
+            reinterpret_cast<uint4*>(tail)[i] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
+        if (threadIdx.x == 0) next_batch = 0;
+        __syncthreads();
+        for (uint32_t j = vb + threadIdx.x; j < ve; j += blockDim.x) {
+            const uint32_t w = radj[j];
+            if (w < kHotBits) atomicOr(&bits[w >> 5], 1u << (w & 31u));
+            else bucket_insert(tail, ntb, w);
+        }
+        __syncthreads();
+        for (;;) {
+            uint32_t bidx = 0;
+            if (lane == 0) bidx = atomicAdd(&next_batch, 1u);
+            const uint32_t kb = tk.e0 + 32u * __shfl_sync(0xFFFFFFFFu, bidx, 0);
+            if (kb >= tk.e1) break;
+            const uint32_t k = kb + lane;
+            const bool valid = k < tk.e1;
+            uint32_t ub = 0, ue = 0;
+            if (valid) {
+                const uint32_t u = lo_adj[k];
+                ub = off[u];
+                ue = off[u + 1];
+            }
+            const uint32_t wa = ub & ~3u;
+            const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
+            uint32_t cnt = 0;
+            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= kLongWords);
+            while (longs) {
+                const int j = __ffs(longs) - 1;
+                longs &= longs - 1;
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
+                const uint32_t c =
+                    __reduce_add_sync(0xFFFFFFFFu, warp_probe_list_bitmap(radj, b, e, bits, tail, ntb, lane));
+                if ((int)lane == j) cnt = c;
+            }
+            const uint32_t sw = nwords < kLongWords ? nwords : 0u;
+            uint32_t incl = sw;
+#pragma unroll
+            for (int s = 1; s < 32; s <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+                if ((int)lane >= s) incl += y;
+            }
+            const uint32_t excl = incl - sw;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t y = base + lane;
+                uint32_t j = 0;
+#pragma unroll
+                for (int s = 16; s > 0; s >>= 1) {
+                    const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
+                    if (pj <= y) j += s;
+                }
+                j &= 31u;
+                const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
+                const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
+                const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, j);
+                const uint32_t le = __shfl_sync(0xFFFFFFFFu, ue, j);
+                uint32_t h = 0;
+                if (y < total) {
+                    const uint32_t p = aj + 4u * (y - ej);
+                    h = bitmap_probe_word(__ldg(reinterpret_cast<const uint4*>(radj + p)), p, lb, le, bits, tail, ntb);
+                }
+                const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
+                const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
+                const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
+                const int lo = (int)min(max((int64_t)excl - (int64_t)base, (int64_t)0), (int64_t)32);
+                const int hi = (int)min(max((int64_t)incl - (int64_t)base, (int64_t)0), (int64_t)32);
+                const uint32_t m = lane_range_mask(lo, hi);
+                cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+            }
+            if (valid) cn[k] = cnt;
+        }
+        __syncthreads();
+        for (uint32_t j = vb + threadIdx.x; j < ve; j += blockDim.x) {   // clear this pivot's bits
+            const uint32_t w = radj[j];
+            if (w < kHotBits) bits[w >> 5] = 0u;
+        }
+        __syncthreads();
+    }
+}
+
+// Task planner.  Pass 1 (outputs null) counts tasks per class; pass 2 writes them.
+// counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks.
+// tail (may be null: bitmap path off) holds each vertex's count of non-hot neighbours.
 struct PlanParams {
-    unsigned long long target_probes;   // probe work per big task
+    unsigned long long target_probes;          // probe work per hash-class task
+    unsigned long long target_probes_bitmap;   // probe work per bitmap task
     uint32_t min_slice_edges;
 };
 
 __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ lo_off,
-                       const unsigned long long* __restrict__ work, PlanParams pp,
-                       uint32_t* __restrict__ counts, uint32_t* __restrict__ small_out,
-                       CnTask* __restrict__ big0, CnTask* __restrict__ big1, CnTask* __restrict__ big2) {
-    __shared__ uint32_t blk[1 + kNumBigClasses];
-    __shared__ uint32_t base[1 + kNumBigClasses];
-    if (threadIdx.x < 1 + kNumBigClasses) blk[threadIdx.x] = 0;
+                       const unsigned long long* __restrict__ work, const uint32_t* __restrict__ tail,
+                       PlanParams pp, uint32_t* __restrict__ counts, uint32_t* __restrict__ small_out,
+                       CnTask* __restrict__ big0, CnTask* __restrict__ big1, CnTask* __restrict__ big2,
+                       CnTask* __restrict__ bmp) {
+    __shared__ uint32_t blk[2 + kNumBigClasses];
+    __shared__ uint32_t base[2 + kNumBigClasses];
+    if (threadIdx.x < 2 + kNumBigClasses) blk[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     int cls = -1;
@@ -296,6 +445,13 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
             if (dv <= kSmallDeg) {
                 cls = 0;
                 ntask = 1;
+            } else if (tail && dv > kBitmapMinDeg && tail[v] <= kTailMax) {
+                cls = 1 + kNumBigClasses;
+                nch = 1;
+                unsigned long long s = (work[v] + pp.target_probes_bitmap - 1) / pp.target_probes_bitmap;
+                const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
+                nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
+                ntask = nsl;
             } else {
                 nch = (dv + kChunkMax - 1) / kChunkMax;
                 const uint32_t ce = (dv + nch - 1) / nch;
@@ -311,7 +467,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
     uint32_t mine = 0;
     if (cls >= 0) mine = atomicAdd(&blk[cls], ntask);
     __syncthreads();
-    if (threadIdx.x < 1 + kNumBigClasses) base[threadIdx.x] = atomicAdd(&counts[threadIdx.x], blk[threadIdx.x]);
+    if (threadIdx.x < 2 + kNumBigClasses) base[threadIdx.x] = atomicAdd(&counts[threadIdx.x], blk[threadIdx.x]);
     __syncthreads();
     if (cls < 0 || (small_out == nullptr)) return;
     const uint32_t pos = base[cls] + mine;
@@ -319,7 +475,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
         small_out[pos] = v;
         return;
     }
-    CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : big2;
+    CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : cls == 3 ? big2 : bmp;
     const uint32_t vb = off[v], e0 = lo_off[v];
     uint32_t i = 0;
     for (uint32_t c = 0; c < nch; ++c) {
@@ -328,7 +484,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
         for (uint32_t s = 0; s < nsl; ++s, ++i) {
             CnTask t;
             t.v = v;
-            t.cb = cb;
+            t.cb = cls == 1 + kNumBigClasses ? tail[v] : cb;
             t.ce = cend;
             t.e0 = e0 + (uint32_t)((uint64_t)L * s / nsl);
             t.e1 = e0 + (uint32_t)((uint64_t)L * (s + 1) / nsl);

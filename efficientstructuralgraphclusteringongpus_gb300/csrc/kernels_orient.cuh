@@ -17,24 +17,32 @@
 
 namespace scan {
 
-// Warp per vertex: number of lower neighbours and their total degree.
+// Warp per vertex: number of lower neighbours and their total degree; with hot ids
+// (may be null), also the number of non-hot neighbours ("tail", bitmap path).
 __global__ void k_count_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                              uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work) {
+                              uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
+                              const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     for (uint64_t v = warp; v < n; v += nwarps) {
         const uint32_t b = off[v], e = off[v + 1], dv = e - b;
-        uint32_t c = 0;
+        uint32_t c = 0, tl = 0;
         unsigned long long w = 0;
         for (uint32_t j = b + lane; j < e; j += 32) {
             const uint32_t u = adj[j];
             const uint32_t du = off[u + 1] - off[u];
             if (precedes(du, u, dv, (uint32_t)v)) { ++c; w += du; }
+            if (hot) tl += hot[u] >= hot_bits;
         }
         c = __reduce_add_sync(0xFFFFFFFFu, c);
+        tl = __reduce_add_sync(0xFFFFFFFFu, tl);
         for (int s = 16; s > 0; s >>= 1) w += __shfl_xor_sync(0xFFFFFFFFu, w, s);
-        if (lane == 0) { cnt[v] = c; work[v] = w; }
+        if (lane == 0) {
+            cnt[v] = c;
+            work[v] = w;
+            if (hot) tail[v] = tl;
+        }
     }
 }
 
@@ -66,6 +74,51 @@ __global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const
             pos += __popc(mask);
         }
     }
+}
+
+// ---- hot ids for the bitmap path -----------------------------------------------------------
+// Degree histogram with exact bins below 1024 and 256-wide bins above (monotone in degree).
+constexpr uint32_t kDegBins = 2048;
+__host__ __device__ __forceinline__ uint32_t deg_bin(uint32_t d) {
+    return d < 1024u ? d : 1024u + min((d - 1024u) >> 8, 1023u);
+}
+
+__global__ void k_deg_hist(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kDegBins];
+    for (uint32_t i = threadIdx.x; i < kDegBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[deg_bin(off[v + 1] - off[v])], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kDegBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// hot[v] in [0, hot_bits) for vertices whose degree bin is >= min_bin (at most hot_bits of
+// them), hot_bits + v otherwise.  The order among hot ids is whatever the atomics give:
+// counts do not depend on it.
+__global__ void k_hot_assign(uint32_t n, const uint32_t* __restrict__ off, uint32_t min_bin, uint32_t hot_bits,
+                             uint32_t* __restrict__ hot, uint32_t* __restrict__ counter) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint64_t v0 = blockIdx.x * (uint64_t)blockDim.x; v0 < n; v0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = v0 + threadIdx.x;
+        bool is_hot = false;
+        if (v < n) {
+            const uint32_t d = off[v + 1] - off[v];
+            is_hot = d > 0 && deg_bin(d) >= min_bin;
+        }
+        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, is_hot);
+        uint32_t base = 0;
+        if (lane == 0 && mask) base = atomicAdd(counter, __popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (v < n) hot[v] = is_hot ? base + __popc(mask & ((1u << lane) - 1u)) : hot_bits + (uint32_t)v;
+    }
+}
+
+__global__ void k_map_adj(uint64_t m, const uint32_t* __restrict__ adj, const uint32_t* __restrict__ hot,
+                          uint32_t* __restrict__ radj) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < m; j += (uint64_t)gridDim.x * blockDim.x)
+        radj[j] = hot[adj[j]];
 }
 
 // ---- exclusive scan of uint32 counts (n items) into out[0..n], out[n] = total ----------

@@ -129,6 +129,12 @@ struct DeviceGraph {
     uint32_t nsmall = 0;
     CnTask* big[kNumBigClasses] = {};
     uint32_t nbig[kNumBigClasses] = {};
+    // bitmap path (null when off)
+    uint32_t* hot = nullptr;       // n: hot id or kHotBits + v
+    uint32_t* radj = nullptr;      // m + pad: adjacency mapped through hot[]
+    uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
+    CnTask* bmp = nullptr;
+    uint32_t nbmp = 0;
     uint32_t* cn = nullptr;
     bool cn_valid = false;
     bool cn_valid_before = false;
@@ -147,7 +153,7 @@ struct DeviceGraph {
     uint32_t* scratch = nullptr;   // scan tile sums, then dflags
     uint32_t* dflags = nullptr;    // [0] input checks, [1..4] planner counters, [8] flatten flag
     std::vector<void*> allocs;
-    cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-11 similarity kernels
+    cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
 };
 
@@ -266,8 +272,41 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     if (bad & kBadSelfLoop) return fail(SCAN_ERR_FORMAT, "self loop");
     if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
 
+    // Hot ids for the bitmap path: the kHotBits highest-degree vertices (by degree bin).
+    // SCAN_GB300_BITMAP=on|off overrides the default ("auto": on when every vertex with an
+    // edge gets a hot id, so no pivot has a tail -- measured faster there; with tails the
+    // hash classes are kept).
+    const char* knob = std::getenv("SCAN_GB300_BITMAP");
+    const int mode = knob && !std::strcmp(knob, "on") ? 1 : knob && !std::strcmp(knob, "off") ? 0 : 2;
+    bool bitmap_path = mode != 0 && n + kHotBits < 0xFFFFFFF0ull && m > 0;
+    uint32_t* hist = nullptr;
+    std::vector<uint32_t> h(kDegBins, 0);
+    uint32_t min_bin = 1;                            // isolated vertices are never hot
+    if (bitmap_path) {
+        SCAN_TRY(dalloc(d.get(), &hist, kDegBins + 1));
+        SCAN_CUDA(cudaMemsetAsync(hist, 0, (kDegBins + 1) * sizeof(uint32_t), s));
+        k_deg_hist<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, hist);
+        SCAN_CUDA(cudaMemcpyAsync(h.data(), hist, kDegBins * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        SCAN_CUDA(cudaStreamSynchronize(s));
+        uint64_t acc = 0;
+        for (uint32_t b = kDegBins; b-- > 1;) {
+            if (acc + h[b] > kHotBits) { min_bin = b + 1; break; }
+            acc += h[b];
+        }
+        if (mode == 2 && min_bin > 1) bitmap_path = false;   // some vertex would have a tail
+    }
+    if (bitmap_path) {
+        SCAN_TRY(dalloc(d.get(), &d->hot, n));
+        SCAN_TRY(dalloc(d.get(), &d->radj, m + kAdjPad));
+        SCAN_TRY(dalloc(d.get(), &d->tailc, n));
+        k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, min_bin, kHotBits, d->hot, hist + kDegBins);
+        k_map_adj<<<grid_for(d.get(), m, 256), 256, 0, s>>>(m, d->adj, d->hot, d->radj);
+        SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s));
+    }
+
     // Orientation.
-    k_count_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, cnt, d->work);
+    k_count_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, cnt, d->work, d->hot, kHotBits,
+                                                                d->tailc);
     SCAN_TRY(device_scan(d.get(), cnt, n, d->lo_off, d->scratch));
     uint32_t E32 = 0;
     SCAN_CUDA(cudaMemcpyAsync(&E32, d->lo_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -282,11 +321,13 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     // Task plan: count, size, fill.
     PlanParams pp;
     pp.target_probes = 1ull << 22;
+    pp.target_probes_bitmap = 1ull << 23;
     pp.min_slice_edges = 64;
     uint32_t* counts = flags + 1;
     const unsigned pg = (unsigned)((n + 255) / 256);
-    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, pp, counts, nullptr, nullptr, nullptr, nullptr);
-    uint32_t hc[1 + kNumBigClasses];
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
+                              nullptr, nullptr);
+    uint32_t hc[2 + kNumBigClasses];
     SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
     d->nsmall = hc[0];
@@ -295,9 +336,11 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
         d->nbig[c] = hc[1 + c];
         SCAN_TRY(dalloc(d.get(), &d->big[c], d->nbig[c]));
     }
+    d->nbmp = hc[1 + kNumBigClasses];
+    SCAN_TRY(dalloc(d.get(), &d->bmp, d->nbmp));
     SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
-    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, pp, counts, d->small_piv, d->big[0], d->big[1],
-                              d->big[2]);
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
+                              d->big[1], d->big[2], d->bmp);
     SCAN_CUDA(cudaGetLastError());
 
     // Result and scratch arrays.
@@ -318,13 +361,14 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     if (st) {
         st->ms_h2d = ev_ms(d->ev[0], d->ev[1]);
         st->ms_orient = ev_ms(d->ev[1], d->ev[2]);
-        st->kernel_launches += 10 + (off64 ? 1 : 0);
+        st->kernel_launches += 10 + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
     }
     *out = d.release();
     return SCAN_OK;
 }
 
 static bool g_attr_set[64] = {};
+static bool g_attr_bitmap[64] = {};
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
 static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
@@ -338,7 +382,8 @@ static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
-    if (d->device >= 0 && d->device < 64 && !g_attr_set[d->device]) {
+    if (d->device < 0 || d->device >= 64) return fail(SCAN_ERR_INVALID_ARG, "device index must be < 64");
+    if (!g_attr_set[d->device]) {
         SCAN_CUDA(cudaFuncSetAttribute(k_cn_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(big_class_slots(kNumBigClasses - 1) * sizeof(uint32_t))));
         g_attr_set[d->device] = true;
@@ -357,6 +402,17 @@ static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
     }
+    if (d->nbmp) {
+        const size_t smem = (kHotBits / 32 + kTailSlots) * sizeof(uint32_t);
+        if (!g_attr_bitmap[d->device]) {
+            SCAN_CUDA(cudaFuncSetAttribute(k_cn_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            g_attr_bitmap[d->device] = true;
+        }
+        const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
+        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->off, d->radj, d->lo_adj, d->cn);
+        ++*launches;
+    }
+    SCAN_CUDA(cudaEventRecord(d->ev[12], s));
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }
@@ -364,8 +420,10 @@ static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
 static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
     st->ms_cn_kernel[0] = ev_ms(d->ev[7], d->ev[8]);
     for (int c = 0; c < kNumBigClasses; ++c) st->ms_cn_kernel[1 + c] = ev_ms(d->ev[8 + c], d->ev[9 + c]);
+    st->ms_cn_kernel[4] = ev_ms(d->ev[11], d->ev[12]);
     st->cn_work_items[0] = d->nsmall;
     for (int c = 0; c < kNumBigClasses; ++c) st->cn_work_items[1 + c] = d->nbig[c];
+    st->cn_work_items[4] = d->nbmp;
 }
 
 // predicate -> cores -> union-find -> attach -> classify, on cached cn.

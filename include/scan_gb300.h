@@ -81,9 +81,9 @@ typedef struct scan_stats {
     double ms_cluster;          /* core flags, union-find, attach, hub/outlier                */
     double ms_d2h;              /* result copies                                              */
     double ms_total;            /* first event to last event of the run                       */
-    double ms_cn_kernel[4];     /* similarity-stage kernels: small-pivot warps, then the three
-                                   shared-memory table classes (1024 / 4096 / 12288 entries)   */
-    uint64_t cn_work_items[4];  /* pivots (small class) or tasks (table classes) of each        */
+    double ms_cn_kernel[5];     /* similarity-stage kernels: small-pivot warps, the three hash
+                                   table classes (1024 / 4096 / 6144 entries), the bitmap path */
+    uint64_t cn_work_items[5];  /* pivots (small class) or tasks (the others) of each           */
     uint32_t kernel_launches;   /* kernels this library launched for the run                  */
     uint32_t reserved;
 } scan_stats;
