@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "ScanError", "Graph", "ScanStats", "GPUScan", "count_clusters", "library_path", "load_library",
-    "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
+    "cores_noalloc", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
 ]
 
 PRED_EXACT = 0
@@ -98,6 +98,8 @@ _SIGS = {
     "scan_gpuscan_compat": (_i32p, [C.c_int64, C.c_int64, _i32p, _u32p, _u32p, _i32p, _i32p, C.c_double, C.c_int]),
     "scan_count_clusters": (C.c_uint64, [_i32p, C.c_uint64]),
     "scan_eps_to_decimal": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
+    "scan_cores_noalloc": (C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, C.c_uint64, C.c_char_p, C.c_int, C.c_int, _vp,
+                                     _vp]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGS)
 
@@ -333,6 +335,18 @@ def GPUScan(num_edges: np.ndarray, adj: np.ndarray, eps: float, miu: int, eid=No
         libc_free.restype = None
         libc_free(C.cast(p, C.c_void_p))
     return out
+
+
+def cores_noalloc(d_offsets: int, n: int, d_edge_u: int, d_edge_v: int, d_cn: int, num_edges: int, eps,
+                  mu: int, predicate: int, d_is_core: int, stream: int = 0) -> None:
+    """Core flags into caller-owned device memory, allocating nothing (scan_cores_noalloc).
+
+    Every buffer argument is a device address (an int, e.g. a tensor's data_ptr()); the
+    work is queued on `stream` and this returns before it completes.  For callers that
+    may not allocate device memory themselves; limited to 2^20 vertices.
+    """
+    _check(load_library().scan_cores_noalloc(d_offsets, n, d_edge_u, d_edge_v, d_cn, num_edges, _eps_text(eps),
+                                             int(mu), int(predicate), d_is_core, stream or None))
 
 
 def count_clusters(label: np.ndarray) -> int:

@@ -177,6 +177,28 @@ int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj,
                              const int32_t* edge_u, const int32_t* edge_v, double eps,
                              int mu);
 
+/* ---- core check without device allocation ------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device memory
+ * themselves: a plugin or custom call whose host framework owns all device memory and only
+ * hands buffers in, a process whose HBM is already committed to resident graphs, or code
+ * that must avoid cudaMalloc/cudaFree because they synchronise the whole device.
+ * Every buffer is the caller's device memory: d_offsets[n+1]; the undirected edges
+ * d_edge_u/d_edge_v[num_edges] (each edge once, either orientation) with their common-
+ * neighbour counts d_cn[num_edges], e.g. from scan_common_neighbors and
+ * scan_orient_reference.  d_is_core[n] receives 1 for a core and 0 otherwise -- the same
+ * answer as role == SCAN_ROLE_CORE from scan_run.  Work is queued on `stream` (a
+ * cudaStream_t; NULL is the default stream) of the current device and the call returns
+ * before it completes.  The per-vertex scratch is a fixed array built into the library
+ * (4 MiB on every GPU that loads it, held until the process exits), so n above 2^20
+ * returns SCAN_ERR_TOO_LARGE.  The first call on a device looks up that array's address:
+ * make it before any stream capture.  All calls share the one array and it keeps the last
+ * call's contents (each call clears what it needs): calls that overlap on the GPU -- other
+ * streams, other host threads -- race and give wrong results, so serialise them. */
+scan_status scan_cores_noalloc(const uint32_t* d_offsets, uint32_t n, const uint32_t* d_edge_u,
+                               const uint32_t* d_edge_v, const uint32_t* d_cn,
+                               uint64_t num_edges, const char* eps_decimal, int mu,
+                               scan_predicate predicate, uint8_t* d_is_core, void* stream);
+
 /* Number of distinct labels >= 0, as printed by the reference CLI (main.cpp:83-111). */
 uint64_t scan_count_clusters(const int32_t* label, uint64_t n);
 
