@@ -19,14 +19,23 @@ namespace scan {
 
 // Warp per vertex: number of lower neighbours and their total degree; with hot ids
 // (may be null), also the number of non-hot neighbours ("tail", bitmap path).
+// Vertices with more than kBigList entries are left to the CTA-per-vertex kernels below
+// (appended to big[] here), so one long list does not hold a warp for the whole pass.
+constexpr uint32_t kBigList = 2048;
+
 __global__ void k_count_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                               uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
-                              const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail) {
+                              const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
+                              uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     for (uint64_t v = warp; v < n; v += nwarps) {
         const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        if (dv > kBigList) {
+            if (lane == 0) big[atomicAdd(nbig, 1u)] = (uint32_t)v;
+            continue;
+        }
         uint32_t c = 0, tl = 0;
         unsigned long long w = 0;
         for (uint32_t j = b + lane; j < e; j += 32) {
@@ -56,6 +65,7 @@ __global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const
     const uint32_t lt = (1u << lane) - 1u;
     for (uint64_t v = warp; v < n; v += nwarps) {
         const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        if (dv > kBigList) continue;
         uint32_t pos = lo_off[v];
         for (uint32_t j0 = b; j0 < e; j0 += 32) {
             const uint32_t j = j0 + lane;
@@ -74,6 +84,117 @@ __global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const
             pos += __popc(mask);
         }
     }
+}
+
+// CTA per long list (vertices collected by k_count_lower): the same counts with a block
+// reduction.
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x, unsigned long long* sh) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    unsigned long long t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+    }
+    __syncthreads();
+    return t;   // valid in thread 0
+}
+
+__global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
+                                  const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                                  uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
+                                  const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail) {
+    __shared__ unsigned long long sh[32];
+    const uint32_t nb = *nbig;
+    for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+        const uint32_t v = big[i];
+        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        unsigned long long c = 0, w = 0, tl = 0;
+        for (uint32_t j = b + threadIdx.x; j < e; j += blockDim.x) {
+            const uint32_t u = adj[j];
+            const uint32_t du = off[u + 1] - off[u];
+            if (precedes(du, u, dv, v)) { ++c; w += du; }
+            if (hot) tl += hot[u] >= hot_bits;
+        }
+        c = block_sum_u64(c, sh);
+        w = block_sum_u64(w, sh);
+        tl = block_sum_u64(tl, sh);
+        if (threadIdx.x == 0) {
+            cnt[v] = (uint32_t)c;
+            work[v] = w;
+            if (hot) tail[v] = (uint32_t)tl;
+        }
+    }
+}
+
+// CTA per long list: lower neighbours written in list order, one tile of blockDim entries
+// at a time (block-wide exclusive scan of the flags).
+__global__ void k_fill_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
+                                 const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                                 const uint32_t* __restrict__ lo_off, uint32_t* __restrict__ lo_adj,
+                                 uint32_t* __restrict__ lo_src) {
+    __shared__ uint32_t warp_cnt[32];
+    __shared__ uint32_t tile_base;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nb = *nbig;
+    for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+        const uint32_t v = big[i];
+        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
+        if (threadIdx.x == 0) tile_base = lo_off[v];
+        __syncthreads();
+        for (uint32_t j0 = b; j0 < e; j0 += blockDim.x) {
+            const uint32_t j = j0 + threadIdx.x;
+            bool low = false;
+            uint32_t u = 0;
+            if (j < e) {
+                u = adj[j];
+                low = precedes(off[u + 1] - off[u], u, dv, v);
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
+            if (lane == 0) warp_cnt[wid] = __popc(mask);
+            __syncthreads();
+            uint32_t before = tile_base, total = 0;
+            for (uint32_t w = 0; w < nw; ++w) {
+                if (w < wid) before += warp_cnt[w];
+                total += warp_cnt[w];
+            }
+            if (low) {
+                const uint32_t p = before + __popc(mask & ((1u << lane) - 1u));
+                lo_adj[p] = u;
+                lo_src[p] = v;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) tile_base += total;
+            __syncthreads();
+        }
+    }
+}
+
+// ---- input checks, entry-parallel -----------------------------------------------------------
+// starts: one bit per adjacency position, set where a non-empty list begins.
+__global__ void k_mark_starts(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ starts) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = off[v];
+        if (off[v + 1] > b) atomicOr(&starts[b >> 5], 1u << (b & 31u));
+    }
+}
+
+// Entry j of some list: its value w is < n; j is not inside w's own list (that would be a
+// self-loop); unless j starts a list, w is above the previous entry.
+__global__ void k_check_entries(uint64_t m, uint32_t n, const uint32_t* __restrict__ off,
+                                const uint32_t* __restrict__ adj, const uint32_t* __restrict__ starts,
+                                uint32_t* __restrict__ bad, uint32_t bad_id, uint32_t bad_loop, uint32_t bad_order) {
+    uint32_t flags = 0;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < m; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = adj[j];
+        if (w >= n) { flags |= bad_id; continue; }
+        if (off[w] <= j && j < off[w + 1]) flags |= bad_loop;
+        const bool start = (starts[j >> 5] >> (j & 31u)) & 1u;
+        if (!start && j > 0 && w <= adj[j - 1]) flags |= bad_order;
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    if (flags && (threadIdx.x & 31) == 0) atomicOr(bad, flags);
 }
 
 // ---- hot ids for the bitmap path -----------------------------------------------------------

@@ -63,27 +63,6 @@ __global__ void k_check_offsets32(const uint32_t* __restrict__ off, uint64_t n, 
     if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != m)) atomicOr(bad, kBadOffsets);
 }
 
-// Warp per vertex: ids in range, no self-loop, strictly ascending (the checks of
-// CheckInputGraph, GPUSCAN++/Graph.cpp:270-288, plus the id range it leaves unchecked).
-__global__ void k_check_lists(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                              uint32_t* __restrict__ bad) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-    uint32_t flags = 0;
-    for (uint64_t v = warp; v < n; v += nwarps) {
-        const uint32_t b = off[v], e = off[v + 1];
-        for (uint32_t j = b + lane; j < e; j += 32) {
-            const uint32_t w = adj[j];
-            if (w >= n) flags |= kBadId;
-            if (w == (uint32_t)v) flags |= kBadSelfLoop;
-            if (j > b && w <= adj[j - 1]) flags |= kBadOrder;
-        }
-    }
-    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
-    if (flags && lane == 0) atomicOr(bad, flags);
-}
-
 __global__ void k_fill_u32(uint32_t* p, uint64_t n, uint32_t x) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = x;
 }
@@ -151,7 +130,7 @@ struct DeviceGraph {
     uint8_t* role = nullptr;
     RunCounters* ctr = nullptr;
     uint32_t* scratch = nullptr;   // scan tile sums, then dflags
-    uint32_t* dflags = nullptr;    // [0] input checks, [1..4] planner counters, [8] flatten flag
+    uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [8] flatten flag, [16] long lists
     std::vector<void*> allocs;
     cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
@@ -265,9 +244,16 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
     if (bad) return fail(SCAN_ERR_FORMAT, "offsets are not a non-decreasing sequence from 0 to m");
-    k_check_lists<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, flags);
-    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    SCAN_CUDA(cudaStreamSynchronize(s));
+    {
+        uint32_t* starts = nullptr;
+        SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
+        SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s));
+        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, starts);
+        k_check_entries<<<grid_for(d.get(), m, 256), 256, 0, s>>>(m, d->n, d->off, d->adj, starts, flags, kBadId,
+                                                                  kBadSelfLoop, kBadOrder);
+        SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        SCAN_CUDA(cudaStreamSynchronize(s));
+    }
     if (bad & kBadId) return fail(SCAN_ERR_FORMAT, "neighbour id >= n");
     if (bad & kBadSelfLoop) return fail(SCAN_ERR_FORMAT, "self loop");
     if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
@@ -304,9 +290,15 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
         SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s));
     }
 
-    // Orientation.
+    // Orientation: warps for short lists, CTAs for the lists k_count_lower sets aside.
+    uint32_t* big_list = nullptr;
+    SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
+    uint32_t* nbig = flags + 16;
+    SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s));
     k_count_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, cnt, d->work, d->hot, kHotBits,
-                                                                d->tailc);
+                                                                d->tailc, big_list, nbig);
+    k_count_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, cnt, d->work, d->hot, kHotBits,
+                                                       d->tailc);
     SCAN_TRY(device_scan(d.get(), cnt, n, d->lo_off, d->scratch));
     uint32_t E32 = 0;
     SCAN_CUDA(cudaMemcpyAsync(&E32, d->lo_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -316,6 +308,7 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
     SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
     k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
+    k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
     SCAN_CUDA(cudaGetLastError());
 
     // Task plan: count, size, fill.
@@ -361,7 +354,7 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
     if (st) {
         st->ms_h2d = ev_ms(d->ev[0], d->ev[1]);
         st->ms_orient = ev_ms(d->ev[1], d->ev[2]);
-        st->kernel_launches += 10 + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
+        st->kernel_launches += 13 + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
     }
     *out = d.release();
     return SCAN_OK;

@@ -176,6 +176,28 @@ def test_gpuscan_compat_matches_oracle():
         assert np.array_equal(out, label)
 
 
+@pytest.mark.parametrize("case,off,adj,msg", [
+    ("self_loop", [0, 2, 3, 4], [0, 1, 0, 1], "self loop"),
+    ("unsorted", [0, 2, 3, 4], [2, 1, 0, 0], "sorted"),
+    ("duplicate", [0, 2, 4], [1, 1, 0, 0], "sorted"),
+    ("id_range", [0, 1, 2], [7, 0], "neighbour id"),
+    ("offsets", [0, 3, 2], [1, 0], "offsets"),
+])
+def test_drop_in_rejects_bad_graphs_on_device(case, off, adj, msg):
+    # GPUScan() does no host-side validation: these are caught by the device checks
+    with pytest.raises(sg.ScanError) as e:
+        sg.GPUScan(np.array(off, np.uint32), np.array(adj, np.int32), 0.5, 2)
+    assert msg in str(e.value)
+
+
+def test_long_lists_orientation_matches_reference_order():
+    # vertices above the long-list threshold take the CTA orientation path
+    g = wheel(5000)
+    eid, eu, ev = g.orient_reference()
+    cn, _ = g.common_neighbors()
+    assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
+
+
 def test_repeat_runs_identical():
     g = sg.Graph.rmat(13, 16, seed=9)
     a = g.run("0.5", 5, EXACT)
