@@ -49,6 +49,12 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-only", action="store_true")
+    ap.add_argument("--serving-graphs", type=int, default=64)
+    ap.add_argument("--serving-min-scale", type=int, default=12)
+    ap.add_argument("--serving-max-scale", type=int, default=18)
+    ap.add_argument("--serving-queries", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -186,6 +192,61 @@ def cpu_baseline(g, eps: str, mu: int, mode: int, seconds: float) -> dict:
                       f"OpenMP on {os.cpu_count()} threads, {dt:.1f} s"}
 
 
+def serving_bench(args, device: int) -> dict:
+    """Served (graph, eps, mu) queries on a resident pool with cached common-neighbour counts,
+    against plain full recompute per query on the same GPU.
+
+    Pool: R-MAT graphs, scales uniform in [min, max] (edge factor 16, seeds 100+i).  Queries:
+    graph uniform, eps uniform in {0.1..0.9}, mu uniform in [2, 20], ref-f64.  Poisson
+    arrivals at 200 / 2,000 / 20,000 queries/s (native replay), plus a saturated run (every
+    query queued at t=0) for the sustainable rate.  Plain recompute: scan_run (similarity +
+    cluster stage) per query, one after another, on a sample of the same queries.
+    """
+    import efficientstructuralgraphclusteringongpus_gb300 as sg
+
+    rng = np.random.default_rng(7)
+    scales = rng.integers(args.serving_min_scale, args.serving_max_scale + 1, args.serving_graphs)
+    graphs = [sg.Graph.rmat(int(sc), 16, seed=100 + i) for i, sc in enumerate(scales)]
+    k = args.serving_queries
+    qg = rng.integers(0, len(graphs), k)
+    qe = [f"0.{d}" for d in rng.integers(1, 10, k)]
+    qm = rng.integers(2, 21, k)
+    qp = np.full(k, sg.PRED_REF_F64)
+    out = {"pool": f"{len(graphs)} R-MAT graphs, scales {args.serving_min_scale}-{args.serving_max_scale} uniform "
+                   f"(edge factor 16), {int(sum(g.num_edges for g in graphs))} undirected edges in total",
+           "queries": k, "predicate": "ref-f64", "rates": []}
+    with sg.Server(device, 8 << 30, 16) as srv:
+        t = time.perf_counter()
+        ids = [srv.add_graph(g) for g in graphs]
+        out["pool_setup_s"] = time.perf_counter() - t
+        gid = [ids[i] for i in qg]
+        srv.replay(gid[:200], qe[:200], qm[:200], qp[:200], np.zeros(min(200, k)))   # warm
+        for rate in (200, 2000, 20000):
+            kk = int(min(k, max(200, rate * 2)))
+            arr = np.cumsum(rng.exponential(1000.0 / rate, kk))
+            lat, st, wall = srv.replay(gid[:kk], qe[:kk], qm[:kk], qp[:kk], arr)
+            ok = st == 0
+            out["rates"].append({"offered_qps": rate, "queries": kk, "achieved_qps": kk / (wall / 1e3),
+                                 "p50_ms": float(np.percentile(lat[ok], 50)), "p99_ms": float(np.percentile(lat[ok], 99)),
+                                 "failed": int((~ok).sum())})
+        lat, st, wall = srv.replay(gid, qe, qm, qp, np.zeros(k))
+        out["saturated"] = {"queries": k, "qps": k / (wall / 1e3), "p50_ms": float(np.percentile(lat, 50)),
+                            "p99_ms": float(np.percentile(lat, 99)), "failed": int((st != 0).sum())}
+        out["server_kernel_launches"] = srv.counters()["kernel_launches"]
+    # plain full recompute per query, sequential, on a sample of the same queries
+    kp = min(k, 200)
+    for i in set(int(x) for x in qg[:kp]):
+        graphs[i].upload(device)
+    graphs[int(qg[0])].run(qe[0], int(qm[0]), sg.PRED_REF_F64, device=device)
+    t = time.perf_counter()
+    for i in range(kp):
+        graphs[int(qg[i])].run(qe[i], int(qm[i]), sg.PRED_REF_F64, device=device)
+    plain_s = time.perf_counter() - t
+    out["plain_recompute_qps"] = kp / plain_s
+    out["speedup_saturated_vs_plain"] = out["saturated"]["qps"] / out["plain_recompute_qps"]
+    return out
+
+
 def reference_arm(args) -> None:
     """The reference path on the host cores.  GPUSCAN++ has no CPU implementation, so the
     oracle port (its restatement) stands in: each step counts common neighbours on a fixed
@@ -247,6 +308,11 @@ def main():
     torch.cuda.set_device(local)
     dist = Dist(world, "nccl")
     mode = sg.PRED_REF_F64 if args.predicate == "ref-f64" else sg.PRED_EXACT
+    if args.serving_only:
+        if rank == 0:
+            print(json.dumps({"metric": "served queries/s", "serving": serving_bench(args, local)}))
+        dist.close()
+        return
 
     g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
     n, E = g.n, g.num_edges
@@ -316,6 +382,7 @@ def main():
         cpu = None
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(g, args.eps, args.mu, mode, args.cpu_seconds)
+        serving = None if args.no_serving else serving_bench(args, local)
         result = {
             "metric": "similarity edges/s", "value": value, "unit": "similarity edges/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -330,6 +397,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
+            "serving": serving,
             "stages_ms": {"similarity": float(np.mean(sim_ms)),
                           "cluster": float(np.mean([s["ms_cluster"] for s in stats])),
                           "d2h": float(np.mean([s["ms_d2h"] for s in stats])),

@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "ScanError", "Graph", "ScanStats", "GPUScan", "count_clusters", "library_path", "load_library",
-    "cores_noalloc", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
+    "cores_noalloc", "Server", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
 ]
 
 PRED_EXACT = 0
@@ -60,6 +60,17 @@ class ScanStats(C.Structure):
             v = getattr(self, name)
             out[name] = list(v) if isinstance(v, C.Array) else v
         return out
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int32), ("graph_id", C.c_uint32), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("device_ms", C.c_double), ("num_cores", C.c_uint64),
+                ("num_clusters", C.c_uint64), ("num_similar_edges", C.c_uint64)]
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in ("submitted", "admitted", "completed", "failed", "pending",
+                                                "in_flight", "graphs", "budget_bytes", "kernel_launches")]
 
 
 _u64p = C.POINTER(C.c_uint64)
@@ -100,6 +111,16 @@ _SIGS = {
     "scan_eps_to_decimal": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
     "scan_cores_noalloc": (C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, C.c_uint64, C.c_char_p, C.c_int, C.c_int, _vp,
                                      _vp]),
+    "scan_server_create": (C.c_int, [C.c_int, C.c_uint64, C.c_uint32, C.POINTER(_vp)]),
+    "scan_server_add_graph": (C.c_int, [_vp, _vp, C.POINTER(C.c_uint32)]),
+    "scan_server_submit": (C.c_int, [_vp, C.c_uint32, C.c_char_p, C.c_int, C.c_int, _i32p, _u8p,
+                                     C.POINTER(C.c_uint64)]),
+    "scan_server_wait": (C.c_int, [_vp, C.c_uint64, C.POINTER(QueryResult)]),
+    "scan_server_poll": (C.c_int, [_vp, C.c_uint64, C.POINTER(C.c_int)]),
+    "scan_server_get_counters": (C.c_int, [_vp, C.POINTER(ServerCounters)]),
+    "scan_server_replay": (C.c_int, [_vp, C.c_uint64, _u32p, C.POINTER(C.c_char_p), _i32p, _i32p,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), _i32p, C.POINTER(C.c_double)]),
+    "scan_server_destroy": (None, [_vp]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGS)
 
@@ -347,6 +368,90 @@ def cores_noalloc(d_offsets: int, n: int, d_edge_u: int, d_edge_v: int, d_cn: in
     """
     _check(load_library().scan_cores_noalloc(d_offsets, n, d_edge_u, d_edge_v, d_cn, num_edges, _eps_text(eps),
                                              int(mu), int(predicate), d_is_core, stream or None))
+
+
+class Server:
+    """Serving loop over resident graphs with cached common-neighbour counts (scan_server_*).
+
+    Queries run only the cluster stage; they are admitted in arrival order as stream slots
+    and the memory budget allow, and run concurrently on the device.
+    """
+
+    def __init__(self, device: int = 0, memory_budget_bytes: int = 1 << 30, max_in_flight: int = 8):
+        h = _vp()
+        _check(load_library().scan_server_create(device, memory_budget_bytes, max_in_flight, C.byref(h)))
+        self._h = h
+        self._n = []
+        self._keep = {}
+
+    def add_graph(self, g: "Graph") -> int:
+        gid = C.c_uint32(0)
+        _check(load_library().scan_server_add_graph(self._h, g._h, C.byref(gid)))
+        self._n.append(g.n)
+        return gid.value
+
+    def submit(self, graph_id: int, eps, mu: int, predicate: int = PRED_EXACT):
+        """Queue a query; returns its ticket.  Results land in buffers kept until wait()."""
+        n = self._n[graph_id]
+        label = np.empty(n, np.int32)
+        role = np.empty(n, np.uint8)
+        t = C.c_uint64(0)
+        _check(load_library().scan_server_submit(self._h, graph_id, _eps_text(eps), int(mu), int(predicate),
+                                                 _ptr(label, C.c_int32), _ptr(role, C.c_uint8), C.byref(t)))
+        self._keep[t.value] = (label, role)
+        return t.value
+
+    def wait(self, ticket: int):
+        """(label, role, result dict) of a ticket; raises ScanError if the query failed."""
+        r = QueryResult()
+        status = load_library().scan_server_wait(self._h, ticket, C.byref(r))
+        label, role = self._keep.pop(ticket)
+        _check(status)
+        return label, role, {name: getattr(r, name) for name, _ in r._fields_}
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int(0)
+        _check(load_library().scan_server_poll(self._h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def counters(self) -> dict:
+        c = ServerCounters()
+        _check(load_library().scan_server_get_counters(self._h, C.byref(c)))
+        return {name: getattr(c, name) for name, _ in c._fields_}
+
+    def replay(self, graph_ids, eps, mus, predicates, arrival_ms):
+        """Submit query i at arrival_ms[i] (native timing); returns (latency_ms, status, wall_ms)."""
+        k = len(graph_ids)
+        gid = np.ascontiguousarray(graph_ids, np.uint32)
+        mu = np.ascontiguousarray(mus, np.int32)
+        pr = np.ascontiguousarray(predicates, np.int32)
+        arr = np.ascontiguousarray(arrival_ms, np.float64)
+        texts = [_eps_text(e) for e in eps]
+        ptrs = (C.c_char_p * max(k, 1))(*texts)
+        lat = np.zeros(max(k, 1), np.float64)
+        st = np.zeros(max(k, 1), np.int32)
+        wall = C.c_double(0)
+        _check(load_library().scan_server_replay(self._h, k, _ptr(gid, C.c_uint32), ptrs, _ptr(mu, C.c_int32),
+                                                 _ptr(pr, C.c_int32), _ptr(arr, C.c_double), _ptr(lat, C.c_double),
+                                                 _ptr(st, C.c_int32), C.byref(wall)))
+        return lat[:k], st[:k], wall.value
+
+    def close(self):
+        if self._h:
+            load_library().scan_server_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def count_clusters(label: np.ndarray) -> int:

@@ -29,8 +29,8 @@ NVCCFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fope
                     "-Xptxas", "-warn-spills"]
 
 CXX_SOURCES = ["graph.cpp", "compat.cpp"]
-CU_SOURCES = ["scan_device.cu", "noalloc.cu"]
-HEADERS = ["graph_internal.h", "device_common.cuh", "predicate.cuh", "kernels_orient.cuh", "kernels_cn.cuh", "kernels_cluster.cuh"]
+CU_SOURCES = ["scan_device.cu", "noalloc.cu", "server.cu"]
+HEADERS = ["graph_internal.h", "device_common.cuh", "device_graph.h", "predicate.cuh", "kernels_orient.cuh", "kernels_cn.cuh", "kernels_cluster.cuh"]
 
 
 def _run(cmd: list[str]) -> None:

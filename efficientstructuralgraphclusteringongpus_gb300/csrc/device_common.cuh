@@ -24,6 +24,9 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t w, uint32_t cap) {
     return __umulhi(w * 0x9E3779B1u, cap);
 }
 
+constexpr int kNumBigClasses = 3;           // hash-table classes of the similarity kernel
+constexpr int kMaxJumpRounds = 40;          // pointer-jumping rounds of the union-find flatten
+
 // Error flags written by bounded device loops.
 constexpr uint32_t kErrUnionFindLimit = 1u;
 constexpr uint32_t kErrHashFull = 2u;

@@ -1,0 +1,91 @@
+// Resident graph and per-run scratch, shared by the translation units that drive the
+// kernels (scan_device.cu: single runs; server.cu: the serving loop).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "device_common.cuh"
+#include "graph_internal.h"
+#include "predicate.cuh"
+
+namespace scan {
+struct CnTask;
+}
+
+// Working arrays of one SCAN pass over a resident graph (cluster stage).  One contiguous
+// block, so a caller can place it anywhere (a plain allocation, or an arena slice in the
+// serving loop); several passes over the same graph can run at once, each with its own.
+struct RunScratch {
+    uint32_t n = 0;
+    uint64_t E = 0;
+    uint8_t* sim = nullptr;        // E: predicate result
+    int32_t* sd = nullptr;         // n: similar-neighbour count
+    int32_t* parent = nullptr;     // n: union-find forest (cores), -1 for non-cores
+    int32_t* bmin = nullptr;       // n: smallest / largest cluster a border is similar to
+    int32_t* bmax = nullptr;
+    int32_t* nmin = nullptr;       // n: smallest / largest label among an unattached vertex's neighbours
+    int32_t* nmax = nullptr;
+    int32_t* lab = nullptr;        // n: label after attachment
+    int32_t* label = nullptr;      // n: final label
+    uint8_t* role = nullptr;       // n: final role
+    scan::RunCounters* ctr = nullptr;
+    uint32_t* jump_flags = nullptr;   // kMaxJumpRounds
+};
+
+struct DeviceGraph {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0;
+    uint64_t m = 0, E = 0;
+    uint32_t* off = nullptr;
+    uint32_t* adj = nullptr;
+    uint32_t* lo_off = nullptr;
+    uint32_t* lo_adj = nullptr;
+    uint32_t* lo_src = nullptr;
+    unsigned long long* work = nullptr;
+    uint32_t* small_piv = nullptr;
+    uint32_t nsmall = 0;
+    scan::CnTask* big[scan::kNumBigClasses] = {};
+    uint32_t nbig[scan::kNumBigClasses] = {};
+    // bitmap path (null when off)
+    uint32_t* hot = nullptr;       // n: hot id or kHotBits + v
+    uint32_t* radj = nullptr;      // m + pad: adjacency mapped through hot[]
+    uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
+    scan::CnTask* bmp = nullptr;
+    uint32_t nbmp = 0;
+    uint32_t* cn = nullptr;        // E: common-neighbour counts (the serving cache)
+    bool cn_valid = false;
+    bool cn_valid_before = false;
+    RunScratch rs;                 // scratch of scan_run on this graph
+    uint32_t* scratch = nullptr;   // scan tile sums, then dflags
+    uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [16] long lists
+    std::vector<void*> allocs;
+    cudaEvent_t ev[16] = {};       // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
+    std::mutex mu;                 // one run at a time per resident graph
+};
+
+namespace scan {
+
+// Bytes of a RunScratch block for n vertices and E edges (256-byte aligned pieces).
+size_t run_scratch_bytes(uint32_t n, uint64_t E);
+// Point r's arrays into `base` (run_scratch_bytes(n, E) bytes of device memory).
+void run_scratch_bind(RunScratch* r, void* base, uint32_t n, uint64_t E);
+
+// Upload a CSR (32- or 64-bit offsets), check it and build the orientation and task plan.
+scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
+                          const uint32_t* adj_host, DeviceGraph** out, scan_stats* st);
+// cn for every edge on d->stream.
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches);
+// predicate -> cores -> union-find -> attach -> classify from d->cn into r, on stream s.
+// No host synchronisation.
+scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
+                           uint32_t* launches);
+// eps text + mode -> predicate parameters.
+scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode);
+
+}  // namespace scan

@@ -100,12 +100,16 @@ __global__ void k_union(uint64_t E, const uint32_t* __restrict__ lo_adj, const u
     }
 }
 
-// Flatten by pointer jumping: parent[v] = parent[parent[v]] for every core, repeated by the
-// host until no pointer changes (O(log depth) rounds).  Every value stored is an ancestor of
-// v in the final forest, so concurrent jumps never undo one another; a find with path
-// halving here would not be safe, because its halving store can overwrite a vertex whose
-// root another thread has just written with an intermediate ancestor.
-__global__ void k_jump(uint32_t n, int32_t* parent, uint32_t* changed) {
+// Flatten by pointer jumping: round r sets parent[v] = parent[parent[v]] for every core and
+// raises flags[r] if any pointer moved.  The host queues enough rounds for any depth
+// (ceil(log2 n) + 2); a round whose predecessor moved nothing returns at once, so the pass
+// needs no host synchronisation.  Every value stored is an ancestor of v in the final
+// forest and only v's own thread writes parent[v], so concurrent jumps never undo one
+// another.  (A find with path halving would not be safe here: its halving store can
+// overwrite a vertex whose root another thread has just written with an intermediate
+// ancestor.)
+__global__ void k_jump_round(uint32_t n, int32_t* parent, uint32_t* flags, uint32_t round) {
+    if (round > 0 && *(volatile uint32_t*)&flags[round - 1] == 0) return;
     volatile int32_t* vp = parent;
     uint32_t ch = 0;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
@@ -117,7 +121,7 @@ __global__ void k_jump(uint32_t n, int32_t* parent, uint32_t* changed) {
             ch = 1;
         }
     }
-    if (__any_sync(0xFFFFFFFFu, ch) && (threadIdx.x & 31) == 0) atomicOr(changed, 1u);
+    if (__any_sync(0xFFFFFFFFu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[round], 1u);
 }
 
 // Border attachment: a non-core similar to a core joins that core's cluster.  The

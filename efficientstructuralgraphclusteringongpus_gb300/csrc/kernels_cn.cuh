@@ -26,7 +26,6 @@ namespace scan {
 constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single warp
 constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
 constexpr uint32_t kChunkMax = 6144;       // max pivot entries staged by one CTA
-constexpr int kNumBigClasses = 3;          // table capacities for chunk sizes below
 // Bitmap path: the kHotBits highest-degree vertices get ids in [0, kHotBits) ("hot");
 // every other vertex x is kHotBits + x.  A pivot's hot neighbours go into a shared-memory
 // bitmap (one bit per hot id, 128 KB), the rest (its "tail") into a bucketed table.

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "device_graph.h"
 #include "graph_internal.h"
 #include "kernels_cluster.cuh"
 #include "kernels_cn.cuh"
@@ -92,50 +93,6 @@ __global__ void k_to_reference_order(uint64_t E, const uint32_t* __restrict__ of
 
 using namespace scan;
 
-struct DeviceGraph {
-    int device = -1;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t n = 0;
-    uint64_t m = 0, E = 0;
-    uint32_t* off = nullptr;
-    uint32_t* adj = nullptr;
-    uint32_t* lo_off = nullptr;
-    uint32_t* lo_adj = nullptr;
-    uint32_t* lo_src = nullptr;
-    unsigned long long* work = nullptr;
-    uint32_t* small_piv = nullptr;
-    uint32_t nsmall = 0;
-    CnTask* big[kNumBigClasses] = {};
-    uint32_t nbig[kNumBigClasses] = {};
-    // bitmap path (null when off)
-    uint32_t* hot = nullptr;       // n: hot id or kHotBits + v
-    uint32_t* radj = nullptr;      // m + pad: adjacency mapped through hot[]
-    uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
-    CnTask* bmp = nullptr;
-    uint32_t nbmp = 0;
-    uint32_t* cn = nullptr;
-    bool cn_valid = false;
-    bool cn_valid_before = false;
-    // per-run scratch
-    uint8_t* sim = nullptr;
-    int32_t* sd = nullptr;
-    int32_t* parent = nullptr;
-    int32_t* bmin = nullptr;
-    int32_t* bmax = nullptr;
-    int32_t* nmin = nullptr;
-    int32_t* nmax = nullptr;
-    int32_t* lab = nullptr;
-    int32_t* label = nullptr;
-    uint8_t* role = nullptr;
-    RunCounters* ctr = nullptr;
-    uint32_t* scratch = nullptr;   // scan tile sums, then dflags
-    uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [8] flatten flag, [16] long lists
-    std::vector<void*> allocs;
-    cudaEvent_t ev[16] = {};   // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
-    std::mutex mu;                 // one run at a time per resident graph
-};
-
 namespace scan {
 
 void device_graph_free(DeviceGraph* d) {
@@ -179,6 +136,45 @@ static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t run_scratch_bytes(uint32_t n, uint64_t E) {
+    return align256(E ? E : 1) + 8 * align256(4ull * n) + align256(n) + align256(sizeof(RunCounters)) +
+           align256(4 * kMaxJumpRounds);
+}
+
+void run_scratch_bind(RunScratch* r, void* base, uint32_t n, uint64_t E) {
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t bytes) { char* q = p; p += align256(bytes); return q; };
+    r->n = n;
+    r->E = E;
+    r->sim = reinterpret_cast<uint8_t*>(take(E ? E : 1));
+    r->sd = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->parent = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->bmin = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->bmax = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->nmin = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->nmax = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->lab = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->label = reinterpret_cast<int32_t*>(take(4ull * n));
+    r->role = reinterpret_cast<uint8_t*>(take(n));
+    r->ctr = reinterpret_cast<RunCounters*>(take(sizeof(RunCounters)));
+    r->jump_flags = reinterpret_cast<uint32_t*>(take(4 * kMaxJumpRounds));
+}
+
+static uint32_t jump_rounds(uint32_t n) {
+    uint32_t r = 2;
+    while ((1ull << (r - 2)) < (uint64_t)n + 1 && r < (uint32_t)kMaxJumpRounds) ++r;
+    return r;
+}
+
+static int grid_for_n(int num_sms, uint64_t items, int threads, int per_sm = 8) {
+    uint64_t g = (items + threads - 1) / threads;
+    uint64_t cap = (uint64_t)num_sms * per_sm;
+    if (g > cap) g = cap;
+    return (int)std::max<uint64_t>(g, 1);
+}
+
 // Exclusive scan of cnt[0..n) into out[0..n] on d->stream (out[n] = total).
 static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, uint32_t* out, uint32_t* sums) {
     const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
@@ -194,7 +190,7 @@ static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, 
 }
 
 // Upload a CSR (32- or 64-bit offsets) and build the lower lists and the task plan.
-static scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
+scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
                                  const uint32_t* adj_host, DeviceGraph** out, scan_stats* st) {
     if (n == 0 || n >= 0xFFFFFFFFull) return fail(SCAN_ERR_INVALID_ARG, "vertex count must be in [1, 2^32-1)");
     if (m >= 0xFFFFFFF0ull) return fail(SCAN_ERR_TOO_LARGE, "m >= 2^32 directed entries");
@@ -338,17 +334,9 @@ static scan_status device_upload(int device, uint64_t n, uint64_t m, const void*
 
     // Result and scratch arrays.
     SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
-    SCAN_TRY(dalloc(d.get(), &d->sim, d->E));
-    SCAN_TRY(dalloc(d.get(), &d->sd, n));
-    SCAN_TRY(dalloc(d.get(), &d->parent, n));
-    SCAN_TRY(dalloc(d.get(), &d->bmin, n));
-    SCAN_TRY(dalloc(d.get(), &d->bmax, n));
-    SCAN_TRY(dalloc(d.get(), &d->nmin, n));
-    SCAN_TRY(dalloc(d.get(), &d->nmax, n));
-    SCAN_TRY(dalloc(d.get(), &d->lab, n));
-    SCAN_TRY(dalloc(d.get(), &d->label, n));
-    SCAN_TRY(dalloc(d.get(), &d->role, n));
-    SCAN_TRY(dalloc(d.get(), &d->ctr, 1));
+    uint8_t* rs_mem = nullptr;
+    SCAN_TRY(dalloc(d.get(), &rs_mem, run_scratch_bytes(d->n, d->E)));
+    run_scratch_bind(&d->rs, rs_mem, d->n, d->E);
     SCAN_CUDA(cudaEventRecord(d->ev[2], s));
     SCAN_CUDA(cudaEventSynchronize(d->ev[2]));
     if (st) {
@@ -364,7 +352,7 @@ static bool g_attr_set[64] = {};
 static bool g_attr_bitmap[64] = {};
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
-static scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
     cudaStream_t s = d->stream;
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaEventRecord(d->ev[7], s));
@@ -419,42 +407,32 @@ static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
     st->cn_work_items[4] = d->nbmp;
 }
 
-// predicate -> cores -> union-find -> attach -> classify, on cached cn.
-static scan_status launch_cluster(DeviceGraph* d, const PredParams& pp, int mu, uint32_t* launches) {
-    cudaStream_t s = d->stream;
+// predicate -> cores -> union-find -> attach -> classify, on cached cn.  Queued on s with
+// no host synchronisation.
+scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
+                           uint32_t* launches) {
     const uint64_t E = d->E;
     const uint32_t n = d->n;
-    SCAN_CUDA(cudaMemsetAsync(d->sd, 0, n * sizeof(int32_t), s));
-    SCAN_CUDA(cudaMemsetAsync(d->ctr, 0, sizeof(RunCounters), s));
-    const int T = 256;
-    k_predicate<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, d->sim, d->sd, d->ctr);
-    k_core_init<<<grid_for(d, n, T), T, 0, s>>>(n, d->sd, mu, d->parent, d->bmin, d->bmax, d->nmin, d->nmax);
-    k_union<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->ctr);
-    *launches += 1;
-    // Flatten: two pointer-jumping rounds per check until nothing changes.
-    uint32_t* changed = d->dflags + 8;
-    for (int round = 0;; ++round) {
-        if (round >= 40) return fail(SCAN_ERR_DEVICE, "union-find flattening did not converge");
-        SCAN_CUDA(cudaMemsetAsync(changed, 0, sizeof(uint32_t), s));
-        k_jump<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, changed);
-        k_jump<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, changed);
-        *launches += 2;
-        uint32_t h = 0;
-        SCAN_CUDA(cudaMemcpyAsync(&h, changed, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        SCAN_CUDA(cudaStreamSynchronize(s));
-        if (!h) break;
-    }
-    k_attach<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->sim, d->parent, d->bmin, d->bmax);
-    k_label<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->lab);
-    k_neighbour_labels<<<grid_for(d, E, T), T, 0, s>>>(E, d->lo_adj, d->lo_src, d->lab, d->nmin, d->nmax);
-    k_finalize<<<grid_for(d, n, T), T, 0, s>>>(n, d->parent, d->bmin, d->bmax, d->nmin, d->nmax, d->label, d->role,
-                                               d->ctr);
-    *launches += 6;
+    const int sms = d->num_sms, T = 256;
+    const int ge = grid_for_n(sms, E, T), gn = grid_for_n(sms, n, T);
+    SCAN_CUDA(cudaMemsetAsync(r.sd, 0, n * sizeof(int32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(r.ctr, 0, sizeof(RunCounters), s));
+    SCAN_CUDA(cudaMemsetAsync(r.jump_flags, 0, kMaxJumpRounds * sizeof(uint32_t), s));
+    k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, r.sim, r.sd, r.ctr);
+    k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
+    k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
+    const uint32_t rounds = jump_rounds(n);
+    for (uint32_t i = 0; i < rounds; ++i) k_jump_round<<<gn, T, 0, s>>>(n, r.parent, r.jump_flags, i);
+    k_attach<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.bmin, r.bmax);
+    k_label<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.lab);
+    k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax);
+    k_finalize<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.bmax, r.nmin, r.nmax, r.label, r.role, r.ctr);
+    *launches += 7 + rounds;
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }
 
-static scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode) {
+scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode) {
     if (!eps_decimal) return fail(SCAN_ERR_INVALID_ARG, "eps text is null");
     uint64_t p = 0, q = 1;
     double e = 0;
@@ -490,16 +468,20 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
     d->cn_valid_before = d->cn_valid;
     if (!(reuse_cn && d->cn_valid)) SCAN_TRY(launch_cn(d, &launches));
     SCAN_CUDA(cudaEventRecord(d->ev[4], s));
-    SCAN_TRY(launch_cluster(d, pp, mu, &launches));
+    SCAN_TRY(launch_cluster(d, d->rs, s, pp, mu, &launches));
     SCAN_CUDA(cudaEventRecord(d->ev[5], s));
     RunCounters hc;
-    if (out_label) SCAN_CUDA(cudaMemcpyAsync(out_label, d->label, d->n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    if (out_role) SCAN_CUDA(cudaMemcpyAsync(out_role, d->role, d->n, cudaMemcpyDeviceToHost, s));
-    SCAN_CUDA(cudaMemcpyAsync(&hc, d->ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    uint32_t last_round = 0;
+    if (out_label) SCAN_CUDA(cudaMemcpyAsync(out_label, d->rs.label, d->n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (out_role) SCAN_CUDA(cudaMemcpyAsync(out_role, d->rs.role, d->n, cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaMemcpyAsync(&hc, d->rs.ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaMemcpyAsync(&last_round, d->rs.jump_flags + jump_rounds(d->n) - 1, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaEventRecord(d->ev[6], s));
     SCAN_CUDA(cudaEventSynchronize(d->ev[6]));
     d->cn_valid = true;
     if (hc.error_flags) return fail(SCAN_ERR_DEVICE, "union-find exceeded its iteration limit");
+    if (last_round) return fail(SCAN_ERR_DEVICE, "union-find flattening did not converge");
     if (st) {
         st->n = d->n;
         st->num_edges = d->E;
@@ -612,7 +594,8 @@ scan_status scan_memberships(scan_graph* g, int device, const char* eps_decimal,
     unsigned long long* cnt = nullptr;
     SCAN_CUDA(cudaMallocAsync(&cnt, sizeof(unsigned long long), s));
     SCAN_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
-    k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->sim, d->parent, cnt, nullptr, 0);
+    k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->rs.sim, d->rs.parent, cnt,
+                                                          nullptr, 0);
     unsigned long long nb = 0;
     SCAN_CUDA(cudaMemcpyAsync(&nb, cnt, sizeof(nb), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
@@ -621,7 +604,8 @@ scan_status scan_memberships(scan_graph* g, int device, const char* eps_decimal,
         unsigned long long* buf = nullptr;
         SCAN_CUDA(cudaMallocAsync(&buf, nb * sizeof(unsigned long long), s));
         SCAN_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
-        k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->sim, d->parent, cnt, buf, nb);
+        k_border_pairs<<<grid_for(d, d->E, 256), 256, 0, s>>>(d->E, d->lo_adj, d->lo_src, d->rs.sim, d->rs.parent, cnt,
+                                                              buf, nb);
         SCAN_CUDA(cudaMemcpyAsync(keys.data(), buf, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         SCAN_CUDA(cudaFreeAsync(buf, s));
     }

@@ -177,6 +177,57 @@ int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj,
                              const int32_t* edge_u, const int32_t* edge_v, double eps,
                              int mu);
 
+/* ---- serving: queries on resident graphs with cached common-neighbour counts ---------
+ * Serves the benchmark spec's serving pattern; the reference has no serving loop.  Each graph
+ * added is uploaded once and its exact cn[] computed once; a query (graph, eps, mu) then runs
+ * only the cluster stage.  Queries are admitted in arrival order when one of max_in_flight
+ * stream slots is free and their scratch fits memory_budget_bytes (reserved on the device at
+ * creation); admitted queries run concurrently on their own streams.  Results are identical
+ * to scan_run on the same graph and parameters, alone or in any mix. */
+typedef struct scan_server scan_server;
+
+typedef struct scan_query_result {
+    uint64_t ticket;
+    int32_t status;             /* scan_status of the query                                 */
+    uint32_t graph_id;
+    double queue_ms;            /* submitted -> admitted                                    */
+    double latency_ms;          /* submitted -> result in the caller's buffers               */
+    double device_ms;           /* cluster stage and result copy on the device (CUDA events)  */
+    uint64_t num_cores;
+    uint64_t num_clusters;
+    uint64_t num_similar_edges;
+} scan_query_result;
+
+typedef struct scan_server_counters {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t pending, in_flight, graphs, budget_bytes;
+    uint64_t kernel_launches;
+} scan_server_counters;
+
+scan_status scan_server_create(int device, uint64_t memory_budget_bytes, uint32_t max_in_flight,
+                               scan_server** out);
+/* Upload g and compute its common-neighbour counts; g may be freed afterwards. */
+scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t* graph_id);
+/* Queue a query; out_label[n] (and out_role[n], may be NULL) are written before the ticket
+ * completes.  Returns at once. */
+scan_status scan_server_submit(scan_server* s, uint32_t graph_id, const char* eps_decimal, int mu,
+                               scan_predicate predicate, int32_t* out_label, uint8_t* out_role,
+                               uint64_t* ticket);
+/* Block until the ticket completes; returns its status and releases the ticket. */
+scan_status scan_server_wait(scan_server* s, uint64_t ticket, scan_query_result* result);
+scan_status scan_server_poll(scan_server* s, uint64_t ticket, int* done);
+scan_status scan_server_get_counters(scan_server* s, scan_server_counters* out);
+/* Load replay: submits query i at arrival_ms[i] after the call starts (one thread sleeps and
+ * spins to the arrival times) while this thread collects results in order.  Fills
+ * latency_ms[i] (submit -> result) and status[i]; *wall_ms (may be NULL) is first arrival ->
+ * last result.  Labels go to internal per-graph buffers: this measures time, not output. */
+scan_status scan_server_replay(scan_server* s, uint64_t num_queries, const uint32_t* graph_id,
+                               const char* const* eps_decimal, const int32_t* mu,
+                               const int32_t* predicate, const double* arrival_ms,
+                               double* latency_ms, int32_t* status, double* wall_ms);
+/* Finishes queued and running queries, then frees everything. */
+void scan_server_destroy(scan_server* s);
+
 /* ---- core check without device allocation ------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory
  * themselves: a plugin or custom call whose host framework owns all device memory and only
