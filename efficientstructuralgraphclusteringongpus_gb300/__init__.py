@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "ScanError", "Graph", "ScanStats", "GPUScan", "count_clusters", "library_path", "load_library",
-    "cores_noalloc", "Server", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
+    "cores_noalloc", "Server", "Batch", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
 ]
 
 PRED_EXACT = 0
@@ -68,6 +68,13 @@ class QueryResult(C.Structure):
                 ("num_clusters", C.c_uint64), ("num_similar_edges", C.c_uint64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("ms_device", C.c_double), ("ms_total", C.c_double)] + [
+        (name, C.c_uint64) for name in ("num_graphs", "num_vertices", "num_edges", "num_cores", "num_clusters")] + [
+        ("graph_kernels", C.c_uint32), ("long_words", C.c_uint32), ("target_probes", C.c_uint64),
+        ("tuned_similarity_ms", C.c_double)]
+
+
 class ServerCounters(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in ("submitted", "admitted", "completed", "failed", "pending",
                                                 "in_flight", "graphs", "budget_bytes", "kernel_launches")]
@@ -97,6 +104,8 @@ _SIGS = {
     "scan_graph_validate": (C.c_int, [_vp, C.c_int]),
     "scan_graph_upload": (C.c_int, [_vp, C.c_int]),
     "scan_graph_release_device": (C.c_int, [_vp]),
+    "scan_graph_upload_streamed": (C.c_int, [_vp, C.c_int, C.c_uint64, _u64p]),
+    "scan_graph_device_bytes": (C.c_uint64, [_vp]),
     "scan_gen_rmat": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_chung_lu": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_sbm": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
@@ -109,8 +118,13 @@ _SIGS = {
     "scan_gpuscan_compat": (_i32p, [C.c_int64, C.c_int64, _i32p, _u32p, _u32p, _i32p, _i32p, C.c_double, C.c_int]),
     "scan_count_clusters": (C.c_uint64, [_i32p, C.c_uint64]),
     "scan_eps_to_decimal": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
+    "scan_graph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint32), _u64p]),
     "scan_cores_noalloc": (C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, C.c_uint64, C.c_char_p, C.c_int, C.c_int, _vp,
                                      _vp]),
+    "scan_batch_create": (C.c_int, [C.POINTER(_vp), C.c_uint32, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "scan_batch_run": (C.c_int, [_vp, C.POINTER(C.c_char_p), _i32p, C.c_int, C.POINTER(_i32p), C.POINTER(_u8p),
+                                 C.POINTER(BatchStats)]),
+    "scan_batch_free": (None, [_vp]),
     "scan_server_create": (C.c_int, [C.c_int, C.c_uint64, C.c_uint32, C.POINTER(_vp)]),
     "scan_server_add_graph": (C.c_int, [_vp, _vp, C.POINTER(C.c_uint32)]),
     "scan_server_submit": (C.c_int, [_vp, C.c_uint32, C.c_char_p, C.c_int, C.c_int, _i32p, _u8p,
@@ -296,6 +310,17 @@ class Graph:
     def upload(self, device: int = 0) -> None:
         _check(load_library().scan_graph_upload(self._h, device))
 
+    def upload_streamed(self, device: int = 0, device_budget_bytes: int = 0) -> int:
+        """Keep the adjacency in pinned host memory read over the host link; the rest on the
+        device under device_budget_bytes (0: no cap).  Returns device bytes used."""
+        used = C.c_uint64(0)
+        _check(load_library().scan_graph_upload_streamed(self._h, device, device_budget_bytes, C.byref(used)))
+        return used.value
+
+    @property
+    def device_bytes(self) -> int:
+        return load_library().scan_graph_device_bytes(self._h)
+
     def release_device(self) -> None:
         _check(load_library().scan_graph_release_device(self._h))
 
@@ -307,6 +332,12 @@ class Graph:
         _check(load_library().scan_run(self._h, device, _eps_text(eps), int(mu), int(predicate),
                                        _ptr(label, C.c_int32), _ptr(role, C.c_uint8), C.byref(st)))
         return ScanResult(label, role, st.as_dict())
+
+    def autotune(self, device: int = 0) -> dict:
+        """Tune the similarity stage (task size x long-list threshold) for later runs."""
+        ms, lw, tp = C.c_double(0), C.c_uint32(0), C.c_uint64(0)
+        _check(load_library().scan_graph_autotune(self._h, device, C.byref(ms), C.byref(lw), C.byref(tp)))
+        return {"similarity_ms": ms.value, "long_words": lw.value, "target_probes": tp.value}
 
     def common_neighbors(self, device: int = 0):
         """cn[E] in the reference edge order, plus stats."""
@@ -368,6 +399,49 @@ def cores_noalloc(d_offsets: int, n: int, d_edge_u: int, d_edge_v: int, d_cn: in
     """
     _check(load_library().scan_cores_noalloc(d_offsets, n, d_edge_u, d_edge_v, d_cn, num_edges, _eps_text(eps),
                                              int(mu), int(predicate), d_is_core, stream or None))
+
+
+class Batch:
+    """Many graphs with their own (eps, mu), one pass: a disjoint union on the device whose
+    similarity and cluster stages run as one captured CUDA graph (scan_batch_*)."""
+
+    def __init__(self, graphs, device: int = 0, autotune: bool = True):
+        self._graphs = list(graphs)   # keep the handles alive
+        arr = (_vp * len(self._graphs))(*[g._h.value for g in self._graphs])
+        h = _vp()
+        _check(load_library().scan_batch_create(arr, len(self._graphs), device, int(autotune), C.byref(h)))
+        self._h = h
+
+    def run(self, eps, mus, predicate: int = PRED_EXACT):
+        """Per-graph (labels, roles) lists and the batch stats dict."""
+        k = len(self._graphs)
+        texts = (C.c_char_p * k)(*[_eps_text(e) for e in eps])
+        mu = np.ascontiguousarray(mus, np.int32)
+        labels = [np.empty(g.n, np.int32) for g in self._graphs]
+        roles = [np.empty(g.n, np.uint8) for g in self._graphs]
+        lp = (_i32p * k)(*[_ptr(x, C.c_int32) for x in labels])
+        rp = (_u8p * k)(*[_ptr(x, C.c_uint8) for x in roles])
+        st = BatchStats()
+        _check(load_library().scan_batch_run(self._h, texts, _ptr(mu, C.c_int32), int(predicate), lp, rp,
+                                             C.byref(st)))
+        return labels, roles, {name: getattr(st, name) for name, _ in st._fields_}
+
+    def close(self):
+        if self._h:
+            load_library().scan_batch_free(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class Server:

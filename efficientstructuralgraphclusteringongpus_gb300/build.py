@@ -29,7 +29,7 @@ NVCCFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fope
                     "-Xptxas", "-warn-spills"]
 
 CXX_SOURCES = ["graph.cpp", "compat.cpp"]
-CU_SOURCES = ["scan_device.cu", "noalloc.cu", "server.cu"]
+CU_SOURCES = ["scan_device.cu", "noalloc.cu", "server.cu", "batch.cu"]
 HEADERS = ["graph_internal.h", "device_common.cuh", "device_graph.h", "predicate.cuh", "kernels_orient.cuh", "kernels_cn.cuh", "kernels_cluster.cuh"]
 
 

@@ -14,6 +14,13 @@
 
 namespace scan {
 struct CnTask;
+
+// Task sizing of the similarity stage (set by the planner; re-planned by the autotuner).
+struct PlanParams {
+    unsigned long long target_probes;          // probe work per hash-class task
+    unsigned long long target_probes_bitmap;   // probe work per bitmap task
+    uint32_t min_slice_edges;
+};
 }
 
 // Working arrays of one SCAN pass over a resident graph (cluster stage).  One contiguous
@@ -58,6 +65,9 @@ struct DeviceGraph {
     uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
     scan::CnTask* bmp = nullptr;
     uint32_t nbmp = 0;
+    uint32_t cap_small = 0, cap_big[scan::kNumBigClasses] = {}, cap_bmp = 0;   // task array capacities
+    scan::PlanParams plan{};
+    uint32_t long_words = 32;      // lists of >= long_words 16-byte words get a whole warp
     uint32_t* cn = nullptr;        // E: common-neighbour counts (the serving cache)
     bool cn_valid = false;
     bool cn_valid_before = false;
@@ -65,6 +75,8 @@ struct DeviceGraph {
     uint32_t* scratch = nullptr;   // scan tile sums, then dflags
     uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [16] long lists
     std::vector<void*> allocs;
+    uint64_t device_bytes = 0;     // device memory held by this graph
+    uint32_t* adj_host = nullptr;  // streamed mode: pinned, GPU-mapped adjacency (adj points into it)
     cudaEvent_t ev[16] = {};       // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
 };
@@ -77,14 +89,30 @@ size_t run_scratch_bytes(uint32_t n, uint64_t E);
 void run_scratch_bind(RunScratch* r, void* base, uint32_t n, uint64_t E);
 
 // Upload a CSR (32- or 64-bit offsets), check it and build the orientation and task plan.
+// adj_in_host_memory: keep the adjacency in pinned, GPU-mapped host memory (the kernels read
+// it over the host link) instead of HBM -- the streamed mode for graphs above a device budget.
 scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
-                          const uint32_t* adj_host, DeviceGraph** out, scan_stats* st);
+                          const uint32_t* adj_host, DeviceGraph** out, scan_stats* st,
+                          bool adj_in_host_memory = false);
 // cn for every edge on d->stream.
 scan_status launch_cn(DeviceGraph* d, uint32_t* launches);
+// Rebuild the similarity tasks for plan parameters pp.
+scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp);
+// Time launch_cn under a few (task size, long-list threshold) settings and keep the fastest;
+// returns the chosen setting's time in *best_ms.
+scan_status autotune_similarity(DeviceGraph* d, float* best_ms);
+// Per-graph parameters of a batched run (many graphs as one disjoint union): the graph of
+// each vertex and each graph's predicate parameters and mu (all device pointers).
+struct BatchParams {
+    const uint32_t* vgid;
+    const PredParams* gpp;
+    const int32_t* gmu;
+};
+
 // predicate -> cores -> union-find -> attach -> classify from d->cn into r, on stream s.
-// No host synchronisation.
+// No host synchronisation.  bp (may be null) gives per-graph parameters.
 scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
-                           uint32_t* launches);
+                           uint32_t* launches, const BatchParams* bp = nullptr);
 // eps text + mode -> predicate parameters.
 scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode);
 

@@ -11,8 +11,11 @@ namespace scan {
 // sim[e] and the similar-degree count sd[] of both endpoints (core rule: a vertex is a
 // core when at least mu of its neighbours are similar, GPUSCAN++/GPUScan.cu:147-165).
 // Edges of one pivot are contiguous, so the pivot side is summed per warp segment.
+// Batched runs (many graphs as one disjoint union) pass vgid[] (graph of each vertex) and
+// per-graph parameters gpp[]; single runs pass null and use pp.
 __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
                             const uint32_t* __restrict__ off, const uint32_t* __restrict__ cn, PredParams pp,
+                            const uint32_t* __restrict__ vgid, const PredParams* __restrict__ gpp,
                             uint8_t* __restrict__ sim, int32_t* __restrict__ sd, RunCounters* __restrict__ ctr) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned long long nsim = 0, ndis = 0;
@@ -26,9 +29,10 @@ __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, con
             v = lo_src[e];
             const uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
             const uint32_t t = cn[e];
-            const bool r = ref_f64_similar(t, du, dv, pp.eps);
-            const bool x = exact_similar(t, du, dv, pp.p, pp.q);
-            s = pp.mode ? r : x;
+            const PredParams P = vgid ? gpp[vgid[u]] : pp;
+            const bool r = ref_f64_similar(t, du, dv, P.eps);
+            const bool x = exact_similar(t, du, dv, P.p, P.q);
+            s = P.mode ? r : x;
             ndis += (r != x);
             nsim += s;
             sim[e] = s;
@@ -49,12 +53,14 @@ __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, con
     }
 }
 
-// parent[v] = v for cores, -1 otherwise; border/neighbour label ranges reset.
-__global__ void k_core_init(uint32_t n, const int32_t* __restrict__ sd, int mu, int32_t* __restrict__ parent,
-                            int32_t* __restrict__ bmin, int32_t* __restrict__ bmax, int32_t* __restrict__ nmin,
-                            int32_t* __restrict__ nmax) {
+// parent[v] = v for cores, -1 otherwise; border/neighbour label ranges reset.  Batched
+// runs pass vgid[] and per-graph gmu[].
+__global__ void k_core_init(uint32_t n, const int32_t* __restrict__ sd, int mu, const uint32_t* __restrict__ vgid,
+                            const int32_t* __restrict__ gmu, int32_t* __restrict__ parent, int32_t* __restrict__ bmin,
+                            int32_t* __restrict__ bmax, int32_t* __restrict__ nmin, int32_t* __restrict__ nmax) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        parent[v] = sd[v] >= mu ? (int32_t)v : -1;
+        const int m = vgid ? gmu[vgid[v]] : mu;
+        parent[v] = sd[v] >= m ? (int32_t)v : -1;
         bmin[v] = 0x7FFFFFFF;
         bmax[v] = -1;
         nmin[v] = 0x7FFFFFFF;

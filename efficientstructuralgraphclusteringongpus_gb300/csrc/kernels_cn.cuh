@@ -20,6 +20,7 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "device_graph.h"
 
 namespace scan {
 
@@ -151,7 +152,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
 //     every round each lane takes one word (a binary search over the batch's prefix sums
 //     names its list), loads it and probes its valid entries, and each edge's owner lane
 //     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
-constexpr uint32_t kLongWords = 32;   // lists of >= 128 entries take the whole warp
+constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
 constexpr int kWordsInFlight = 2;
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
@@ -189,7 +190,7 @@ __device__ __forceinline__ uint32_t warp_probe_list(const uint32_t* __restrict__
 
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                         const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+                         const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words) {
     extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch;
     const uint32_t lane = threadIdx.x & 31;
@@ -226,7 +227,7 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
             const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
             uint32_t cnt = 0;
             // long lists: the whole warp, one list at a time
-            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= kLongWords);
+            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= long_words);
             while (longs) {
                 const int j = __ffs(longs) - 1;
                 longs &= longs - 1;
@@ -235,7 +236,7 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 if ((int)lane == j) cnt = c;
             }
             // short lists: one stream of words
-            const uint32_t sw = nwords < kLongWords ? nwords : 0u;
+            const uint32_t sw = nwords < long_words ? nwords : 0u;
             uint32_t incl = sw;
 #pragma unroll
             for (int s = 1; s < 32; s <<= 1) {
@@ -321,7 +322,8 @@ __device__ __forceinline__ uint32_t warp_probe_list_bitmap(const uint32_t* __res
 // task.cb carries the pivot's tail size.
 __global__ void __launch_bounds__(kBitmapThreads, 1)
 k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ off,
-            const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+            const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn,
+            uint32_t long_words) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* bits = smem;                              // kHotBits / 32 words
     uint32_t* tail = smem + kHotBits / 32;              // kTailSlots words
@@ -361,7 +363,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* _
             const uint32_t wa = ub & ~3u;
             const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
             uint32_t cnt = 0;
-            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= kLongWords);
+            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= long_words);
             while (longs) {
                 const int j = __ffs(longs) - 1;
                 longs &= longs - 1;
@@ -370,7 +372,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* _
                     __reduce_add_sync(0xFFFFFFFFu, warp_probe_list_bitmap(radj, b, e, bits, tail, ntb, lane));
                 if ((int)lane == j) cnt = c;
             }
-            const uint32_t sw = nwords < kLongWords ? nwords : 0u;
+            const uint32_t sw = nwords < long_words ? nwords : 0u;
             uint32_t incl = sw;
 #pragma unroll
             for (int s = 1; s < 32; s <<= 1) {
@@ -419,11 +421,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* _
 // Task planner.  Pass 1 (outputs null) counts tasks per class; pass 2 writes them.
 // counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks.
 // tail (may be null: bitmap path off) holds each vertex's count of non-hot neighbours.
-struct PlanParams {
-    unsigned long long target_probes;          // probe work per hash-class task
-    unsigned long long target_probes_bitmap;   // probe work per bitmap task
-    uint32_t min_slice_edges;
-};
+// (PlanParams: device_graph.h.)
 
 __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ lo_off,
                        const unsigned long long* __restrict__ work, const uint32_t* __restrict__ tail,

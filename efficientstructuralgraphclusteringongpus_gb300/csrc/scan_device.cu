@@ -102,6 +102,7 @@ void device_graph_free(DeviceGraph* d) {
     if (d->device >= 0) cudaSetDevice(d->device);
     if (d->stream) cudaStreamSynchronize(d->stream);
     for (void* p : d->allocs) cudaFree(p);
+    if (d->adj_host) cudaFreeHost(d->adj_host);
     for (auto& e : d->ev)
         if (e) cudaEventDestroy(e);
     if (d->stream) cudaStreamDestroy(d->stream);
@@ -119,6 +120,7 @@ static scan_status dalloc(DeviceGraph* d, T** p, uint64_t count) {
                                                 " bytes failed: " + cudaGetErrorString(err));
     }
     d->allocs.push_back(q);
+    d->device_bytes += std::max<uint64_t>(count, 1) * sizeof(T);
     *p = static_cast<T*>(q);
     return SCAN_OK;
 }
@@ -190,8 +192,43 @@ static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, 
 }
 
 // Upload a CSR (32- or 64-bit offsets) and build the lower lists and the task plan.
+// Build the similarity tasks for plan parameters pp (again on every call: the autotuner
+// re-plans with other task sizes).  Needs the orientation (lo_off, work, tailc).
+scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
+    cudaStream_t s = d->stream;
+    uint32_t* counts = d->dflags + 1;
+    const unsigned pg = (unsigned)((d->n + 255) / 256);
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, (2 + kNumBigClasses) * sizeof(uint32_t), s));
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
+                              nullptr, nullptr);
+    uint32_t hc[2 + kNumBigClasses];
+    SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    // task arrays: reuse the current ones when large enough
+    auto ensure = [&](auto** p, uint32_t* cap, uint32_t need) -> scan_status {
+        if (*p && *cap >= need) return SCAN_OK;
+        SCAN_TRY(dalloc(d, p, need));
+        *cap = need;
+        return SCAN_OK;
+    };
+    d->nsmall = hc[0];
+    SCAN_TRY(ensure(&d->small_piv, &d->cap_small, d->nsmall));
+    for (int c = 0; c < kNumBigClasses; ++c) {
+        d->nbig[c] = hc[1 + c];
+        SCAN_TRY(ensure(&d->big[c], &d->cap_big[c], d->nbig[c]));
+    }
+    d->nbmp = hc[1 + kNumBigClasses];
+    SCAN_TRY(ensure(&d->bmp, &d->cap_bmp, d->nbmp));
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
+    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
+                              d->big[1], d->big[2], d->bmp);
+    SCAN_CUDA(cudaGetLastError());
+    d->plan = pp;
+    return SCAN_OK;
+}
+
 scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_host, bool off64,
-                                 const uint32_t* adj_host, DeviceGraph** out, scan_stats* st) {
+                          const uint32_t* adj_host, DeviceGraph** out, scan_stats* st, bool adj_in_host_memory) {
     if (n == 0 || n >= 0xFFFFFFFFull) return fail(SCAN_ERR_INVALID_ARG, "vertex count must be in [1, 2^32-1)");
     if (m >= 0xFFFFFFF0ull) return fail(SCAN_ERR_TOO_LARGE, "m >= 2^32 directed entries");
     SCAN_CUDA(cudaSetDevice(device));
@@ -205,7 +242,12 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     cudaStream_t s = d->stream;
 
     SCAN_TRY(dalloc(d.get(), &d->off, n + 1));
-    SCAN_TRY(dalloc(d.get(), &d->adj, m + kAdjPad));
+    if (adj_in_host_memory) {
+        SCAN_CUDA(cudaHostAlloc(&d->adj_host, (m + kAdjPad) * sizeof(uint32_t), cudaHostAllocMapped));
+        SCAN_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&d->adj), d->adj_host, 0));
+    } else {
+        SCAN_TRY(dalloc(d.get(), &d->adj, m + kAdjPad));
+    }
     SCAN_TRY(dalloc(d.get(), &d->lo_off, n + 1));
     SCAN_TRY(dalloc(d.get(), &d->work, n));
     const uint64_t tiles = (n + 1 + kScanTile - 1) / kScanTile;
@@ -230,8 +272,13 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     } else {
         SCAN_CUDA(cudaMemcpyAsync(d->off, off_host, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     }
-    SCAN_CUDA(cudaMemcpyAsync(d->adj, adj_host, m * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    SCAN_CUDA(cudaMemsetAsync(d->adj + m, 0, kAdjPad * sizeof(uint32_t), s));
+    if (adj_in_host_memory) {
+        std::memcpy(d->adj_host, adj_host, m * sizeof(uint32_t));
+        std::memset(d->adj_host + m, 0, kAdjPad * sizeof(uint32_t));
+    } else {
+        SCAN_CUDA(cudaMemcpyAsync(d->adj, adj_host, m * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        SCAN_CUDA(cudaMemsetAsync(d->adj + m, 0, kAdjPad * sizeof(uint32_t), s));
+    }
     SCAN_CUDA(cudaEventRecord(d->ev[1], s));
 
     // Input checks first: the orientation kernels index by neighbour id.
@@ -260,7 +307,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     // hash classes are kept).
     const char* knob = std::getenv("SCAN_GB300_BITMAP");
     const int mode = knob && !std::strcmp(knob, "on") ? 1 : knob && !std::strcmp(knob, "off") ? 0 : 2;
-    bool bitmap_path = mode != 0 && n + kHotBits < 0xFFFFFFF0ull && m > 0;
+    bool bitmap_path = mode != 0 && n + kHotBits < 0xFFFFFFF0ull && m > 0 && !adj_in_host_memory;
     uint32_t* hist = nullptr;
     std::vector<uint32_t> h(kDegBins, 0);
     uint32_t min_bin = 1;                            // isolated vertices are never hot
@@ -307,30 +354,12 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
     SCAN_CUDA(cudaGetLastError());
 
-    // Task plan: count, size, fill.
+    // Task plan.
     PlanParams pp;
     pp.target_probes = 1ull << 22;
     pp.target_probes_bitmap = 1ull << 23;
     pp.min_slice_edges = 64;
-    uint32_t* counts = flags + 1;
-    const unsigned pg = (unsigned)((n + 255) / 256);
-    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
-                              nullptr, nullptr);
-    uint32_t hc[2 + kNumBigClasses];
-    SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
-    SCAN_CUDA(cudaStreamSynchronize(s));
-    d->nsmall = hc[0];
-    SCAN_TRY(dalloc(d.get(), &d->small_piv, d->nsmall));
-    for (int c = 0; c < kNumBigClasses; ++c) {
-        d->nbig[c] = hc[1 + c];
-        SCAN_TRY(dalloc(d.get(), &d->big[c], d->nbig[c]));
-    }
-    d->nbmp = hc[1 + kNumBigClasses];
-    SCAN_TRY(dalloc(d.get(), &d->bmp, d->nbmp));
-    SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
-    k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
-                              d->big[1], d->big[2], d->bmp);
-    SCAN_CUDA(cudaGetLastError());
+    SCAN_TRY(plan_tasks(d.get(), pp));
 
     // Result and scratch arrays.
     SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
@@ -350,6 +379,8 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 
 static bool g_attr_set[64] = {};
 static bool g_attr_bitmap[64] = {};
+static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class (found once per device,
+                                                // so capturing launch_cn into a graph queries nothing)
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
 scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
@@ -373,12 +404,14 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
         if (d->nbig[c]) {
             const int threads = c == 0 ? 256 : 512;
             const size_t smem = big_class_slots(c) * sizeof(uint32_t);
-            int per_sm = 1;
-            SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
-            per_sm = std::max(per_sm, 1);
+            int& per_sm = g_per_sm[d->device][c];
+            if (per_sm == 0) {
+                SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
+                per_sm = std::max(per_sm, 1);
+            }
             const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
             k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off,
-                                                            d->adj, d->lo_adj, d->cn);
+                                                            d->adj, d->lo_adj, d->cn, d->long_words);
             ++*launches;
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
@@ -390,11 +423,44 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
             g_attr_bitmap[d->device] = true;
         }
         const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
-        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->off, d->radj, d->lo_adj, d->cn);
+        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->off, d->radj, d->lo_adj, d->cn,
+                                                                  d->long_words);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
     SCAN_CUDA(cudaGetLastError());
+    return SCAN_OK;
+}
+
+// Autotuner: try task sizes x long-list thresholds on this graph, keep the fastest.
+scan_status autotune_similarity(DeviceGraph* d, float* best_ms) {
+    const PlanParams base = d->plan;
+    const unsigned long long probes[] = {1ull << 20, 1ull << 22, 1ull << 24};
+    const uint32_t longs[] = {16, 32, 64};
+    float best = 3.4e38f;
+    PlanParams best_pp = base;
+    uint32_t best_lw = d->long_words;
+    for (unsigned long long tp : probes) {
+        PlanParams pp = base;
+        pp.target_probes = tp;
+        pp.target_probes_bitmap = 2 * tp;
+        SCAN_TRY(plan_tasks(d, pp));
+        for (uint32_t lw : longs) {
+            d->long_words = lw;
+            uint32_t launches = 0;
+            SCAN_TRY(launch_cn(d, &launches));   // warm
+            SCAN_CUDA(cudaEventRecord(d->ev[13], d->stream));
+            SCAN_TRY(launch_cn(d, &launches));
+            SCAN_CUDA(cudaEventRecord(d->ev[14], d->stream));
+            SCAN_CUDA(cudaEventSynchronize(d->ev[14]));
+            const float ms = ev_ms(d->ev[13], d->ev[14]);
+            if (ms < best) { best = ms; best_pp = pp; best_lw = lw; }
+        }
+    }
+    SCAN_TRY(plan_tasks(d, best_pp));
+    d->long_words = best_lw;
+    d->cn_valid = false;
+    if (best_ms) *best_ms = best;
     return SCAN_OK;
 }
 
@@ -410,7 +476,7 @@ static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
 // predicate -> cores -> union-find -> attach -> classify, on cached cn.  Queued on s with
 // no host synchronisation.
 scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
-                           uint32_t* launches) {
+                           uint32_t* launches, const BatchParams* bp) {
     const uint64_t E = d->E;
     const uint32_t n = d->n;
     const int sms = d->num_sms, T = 256;
@@ -418,8 +484,10 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     SCAN_CUDA(cudaMemsetAsync(r.sd, 0, n * sizeof(int32_t), s));
     SCAN_CUDA(cudaMemsetAsync(r.ctr, 0, sizeof(RunCounters), s));
     SCAN_CUDA(cudaMemsetAsync(r.jump_flags, 0, kMaxJumpRounds * sizeof(uint32_t), s));
-    k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, r.sim, r.sd, r.ctr);
-    k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
+    const uint32_t* vgid = bp ? bp->vgid : nullptr;
+    k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr, r.sim, r.sd,
+                                 r.ctr);
+    k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
     k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
     const uint32_t rounds = jump_rounds(n);
     for (uint32_t i = 0; i < rounds; ++i) k_jump_round<<<gn, T, 0, s>>>(n, r.parent, r.jump_flags, i);
@@ -513,6 +581,33 @@ scan_status scan_graph_upload(scan_graph* g, int device) {
     return ensure_device(g, device, nullptr);
 }
 
+scan_status scan_graph_upload_streamed(scan_graph* g, int device, uint64_t device_budget_bytes,
+                                       uint64_t* device_bytes_used) {
+    clear_error();
+    if (!g || device < 0) return fail(SCAN_ERR_INVALID_ARG, "graph is null or device < 0");
+    if (g->dev) { device_graph_free(g->dev); g->dev = nullptr; }
+    // device footprint: offsets, orientation, cn, run scratch, tasks (the adjacency stays on the host)
+    const uint64_t E = g->m / 2;
+    const uint64_t est = 4 * (g->n + 1) * 2 + 8 * g->n + 4 * g->n + 12 * E + run_scratch_bytes((uint32_t)g->n, E) +
+                         (16ull << 20);
+    if (device_budget_bytes && est > device_budget_bytes)
+        return fail(SCAN_ERR_OUT_OF_MEMORY, "streamed graph needs about " + std::to_string(est >> 20) +
+                                                " MiB of device memory, above the budget of " +
+                                                std::to_string(device_budget_bytes >> 20) + " MiB");
+    SCAN_TRY(device_upload(device, g->n, g->m, g->off.data(), true, g->adj.data(), &g->dev, nullptr, true));
+    if (device_bytes_used) *device_bytes_used = g->dev->device_bytes;
+    if (device_budget_bytes && g->dev->device_bytes > device_budget_bytes) {
+        const uint64_t used = g->dev->device_bytes;
+        device_graph_free(g->dev);
+        g->dev = nullptr;
+        return fail(SCAN_ERR_OUT_OF_MEMORY, "streamed graph used " + std::to_string(used >> 20) +
+                                                " MiB of device memory, above the budget");
+    }
+    return SCAN_OK;
+}
+
+uint64_t scan_graph_device_bytes(const scan_graph* g) { return g && g->dev ? g->dev->device_bytes : 0; }
+
 scan_status scan_graph_release_device(scan_graph* g) {
     clear_error();
     if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
@@ -530,6 +625,22 @@ scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
     if (stats) std::memset(stats, 0, sizeof(*stats));
     SCAN_TRY(ensure_device(g, device, stats));
     return run_resident(g->dev, pp, mu, false, out_label, out_role, stats);
+}
+
+scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similarity_ms, uint32_t* long_words,
+                                uint64_t* target_probes) {
+    clear_error();
+    if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
+    SCAN_TRY(ensure_device(g, device, nullptr));
+    DeviceGraph* d = g->dev;
+    std::lock_guard<std::mutex> lock(d->mu);
+    SCAN_CUDA(cudaSetDevice(d->device));
+    float ms = 0.f;
+    SCAN_TRY(autotune_similarity(d, &ms));
+    if (best_similarity_ms) *best_similarity_ms = ms;
+    if (long_words) *long_words = d->long_words;
+    if (target_probes) *target_probes = d->plan.target_probes;
+    return SCAN_OK;
 }
 
 scan_status scan_common_neighbors(scan_graph* g, int device, uint32_t* out_cn, scan_stats* stats) {

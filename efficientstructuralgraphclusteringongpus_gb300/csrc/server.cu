@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -87,6 +88,7 @@ class Arena {
 struct Query {
     uint64_t ticket = 0;
     uint32_t gid = 0;
+    DeviceGraph* graph = nullptr;    // captured under the lock at submission
     PredParams pp{};
     int mu = 0;
     int32_t* out_label = nullptr;
@@ -109,7 +111,8 @@ struct Slot {
     RunCounters* h_ctr = nullptr;
     uint32_t* h_flag = nullptr;
     uint32_t n_cap = 0;
-    bool gpu_done = false;
+    std::atomic<bool> gpu_done{false};
+    bool launching = false;          // assigned to q, CUDA work being queued (outside the lock)
 };
 
 }  // namespace
@@ -135,13 +138,15 @@ struct scan_server {
 
 namespace {
 
+// Runs on the CUDA callback thread.  It only flips an atomic flag and wakes the scheduler;
+// the brief lock makes the wake-up race-free (the scheduler tests its predicate under the
+// lock).  No thread holds the lock while it is inside a CUDA call, so this never waits on
+// a thread that is itself waiting for the device.
 void CUDART_CB on_slot_done(void* arg) {
     auto* pair = static_cast<std::pair<scan_server*, Slot*>*>(arg);
     scan_server* s = pair->first;
-    {
-        std::lock_guard<std::mutex> lock(s->mu);
-        pair->second->gpu_done = true;
-    }
+    pair->second->gpu_done.store(true);
+    { std::lock_guard<std::mutex> lock(s->mu); }
     s->cv_work.notify_one();
     delete pair;
 }
@@ -152,14 +157,14 @@ uint32_t jump_flag_index(uint32_t n) {
     return r - 1;
 }
 
-// Launch q on slot sl (scheduler thread, lock held).
-void launch_query(scan_server* s, Slot& sl, Query* q) {
-    DeviceGraph* g = s->graphs[q->gid];
+// Queue q's work on slot sl (scheduler thread, lock NOT held: CUDA calls only here).
+// Returns the number of kernels launched.
+uint32_t launch_query(scan_server* s, Slot& sl, Query* q) {
+    DeviceGraph* g = q->graph;
     RunScratch r;
     run_scratch_bind(&r, s->arena_base + sl.arena_off, g->n, g->E);
     uint32_t launches = 0;
     cudaStream_t st = sl.stream;
-    sl.gpu_done = false;
     cudaEventRecord(sl.ev_start, st);
     scan_status rc = launch_cluster(g, r, st, q->pp, q->mu, &launches);
     cudaMemcpyAsync(sl.h_label, r.label, g->n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
@@ -171,91 +176,118 @@ void launch_query(scan_server* s, Slot& sl, Query* q) {
     if (rc != SCAN_OK || err != cudaSuccess) {
         q->status = rc != SCAN_OK ? rc : SCAN_ERR_CUDA;
         q->error = rc != SCAN_OK ? scan_last_error() : cudaGetErrorString(err);
-        if (err != cudaSuccess) sl.gpu_done = true;   // no callback will come
+        if (err != cudaSuccess) sl.gpu_done.store(true);   // no callback will come
     }
-    s->totals.kernel_launches += launches;
+    return launches;
 }
 
+bool slot_finished(const Slot& sl) { return sl.q && !sl.launching && sl.gpu_done.load(); }
+
+// The scheduler.  Under the lock it only does bookkeeping (which slots finished, which
+// queries to admit, arena blocks); result copies and every CUDA call happen with the lock
+// released, so a device-wide synchronisation elsewhere in the process (cudaMalloc/cudaFree
+// by another thread) can always drain the host callbacks it waits for.
 void scheduler(scan_server* s) {
     cudaSetDevice(s->device);
-    std::unique_lock<std::mutex> lock(s->mu);
     for (;;) {
-        bool progressed = false;
-        // retire finished slots
-        for (Slot& sl : s->slots) {
-            if (!sl.q || !sl.gpu_done) continue;
-            Query* q = sl.q;
-            DeviceGraph* g = s->graphs[q->gid];
+        std::vector<Slot*> finished;
+        std::vector<Slot*> to_launch;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_work.wait(lock, [&] {
+                bool any_busy = false;
+                for (Slot& sl : s->slots) {
+                    if (slot_finished(sl)) return true;
+                    any_busy |= sl.q != nullptr;
+                }
+                if (s->stop && !any_busy && s->pending.empty()) return true;
+                if (s->pending.empty() || s->mem_blocked || s->pause_admission) return false;
+                for (Slot& sl : s->slots)
+                    if (!sl.q) return true;
+                return false;
+            });
+            for (Slot& sl : s->slots)
+                if (slot_finished(sl)) finished.push_back(&sl);
+            bool any_busy = false;
+            for (Slot& sl : s->slots) any_busy |= sl.q != nullptr;
+            if (s->stop && !any_busy && s->pending.empty()) return;
+        }
+        // results out of the pinned staging (no lock; these slots are not touched elsewhere)
+        for (Slot* sl : finished) {
+            Query* q = sl->q;
+            DeviceGraph* g = q->graph;
             float ms = 0.f;
-            cudaEventElapsedTime(&ms, sl.ev_start, sl.ev_end);
+            cudaEventElapsedTime(&ms, sl->ev_start, sl->ev_end);
             q->device_ms = ms;
-            q->counters = *sl.h_ctr;
-            if (q->status == SCAN_OK && (q->counters.error_flags || *sl.h_flag)) {
+            q->counters = *sl->h_ctr;
+            if (q->status == SCAN_OK && (q->counters.error_flags || *sl->h_flag)) {
                 q->status = SCAN_ERR_DEVICE;
                 q->error = "union-find did not finish within its limits";
             }
             if (q->status == SCAN_OK) {
-                std::memcpy(q->out_label, sl.h_label, g->n * sizeof(int32_t));
-                if (q->out_role) std::memcpy(q->out_role, sl.h_role, g->n);
+                std::memcpy(q->out_label, sl->h_label, g->n * sizeof(int32_t));
+                if (q->out_role) std::memcpy(q->out_role, sl->h_role, g->n);
             }
-            s->arena.release(sl.arena_off, sl.arena_bytes);
-            s->mem_blocked = false;
-            sl.q = nullptr;
-            q->finished = Clock::now();
-            q->done = true;
-            ++s->totals.completed;
-            if (q->status != SCAN_OK) ++s->totals.failed;
-            progressed = true;
         }
-        if (progressed) s->cv_done.notify_all();
-        // admit in arrival order while a slot is free and the scratch fits
-        while (!s->pending.empty() && !s->pause_admission) {
-            Query* q = s->pending.front();
-            DeviceGraph* g = s->graphs[q->gid];
-            const uint64_t need = run_scratch_bytes(g->n, g->E);
-            if (need > s->arena.size()) {   // can never fit
-                s->pending.pop_front();
-                q->status = SCAN_ERR_OUT_OF_MEMORY;
-                q->error = "query scratch exceeds the server's memory budget";
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            for (Slot* sl : finished) {
+                Query* q = sl->q;
+                s->arena.release(sl->arena_off, sl->arena_bytes);
+                s->mem_blocked = false;
+                sl->q = nullptr;
                 q->finished = Clock::now();
                 q->done = true;
                 ++s->totals.completed;
-                ++s->totals.failed;
-                s->cv_done.notify_all();
-                continue;
+                if (q->status != SCAN_OK) ++s->totals.failed;
             }
-            Slot* free_slot = nullptr;
-            for (Slot& sl : s->slots)
-                if (!sl.q) { free_slot = &sl; break; }
-            uint64_t off = 0;
-            if (!free_slot) break;
-            if (!s->arena.alloc(need, &off)) {
-                s->mem_blocked = true;   // admitted again once a running query returns its block
-                break;
+            // admit in arrival order while a slot is free and the scratch fits
+            while (!s->pending.empty() && !s->pause_admission) {
+                Query* q = s->pending.front();
+                DeviceGraph* g = q->graph;
+                const uint64_t need = run_scratch_bytes(g->n, g->E);
+                if (need > s->arena.size()) {   // can never fit
+                    s->pending.pop_front();
+                    q->status = SCAN_ERR_OUT_OF_MEMORY;
+                    q->error = "query scratch exceeds the server's memory budget";
+                    q->finished = Clock::now();
+                    q->done = true;
+                    ++s->totals.completed;
+                    ++s->totals.failed;
+                    finished.push_back(nullptr);   // waiters to wake
+                    continue;
+                }
+                Slot* free_slot = nullptr;
+                for (Slot& sl : s->slots)
+                    if (!sl.q) { free_slot = &sl; break; }
+                if (!free_slot) break;
+                uint64_t off = 0;
+                if (!s->arena.alloc(need, &off)) {
+                    s->mem_blocked = true;   // admitted again once a running query returns its block
+                    break;
+                }
+                s->pending.pop_front();
+                free_slot->q = q;
+                free_slot->arena_off = off;
+                free_slot->arena_bytes = need;
+                free_slot->gpu_done.store(false);
+                free_slot->launching = true;
+                q->admitted = Clock::now();
+                ++s->totals.admitted;
+                to_launch.push_back(free_slot);
             }
-            s->pending.pop_front();
-            free_slot->q = q;
-            free_slot->arena_off = off;
-            free_slot->arena_bytes = need;
-            q->admitted = Clock::now();
-            launch_query(s, *free_slot, q);
-            ++s->totals.admitted;
         }
-        bool busy = false;
-        for (Slot& sl : s->slots) busy |= sl.q != nullptr;
-        if (!busy) s->cv_done.notify_all();   // a graph being added waits for idle slots
-        if (s->stop && !busy && s->pending.empty()) return;
-        s->cv_work.wait(lock, [&] {
-            for (Slot& sl : s->slots)
-                if (sl.q && sl.gpu_done) return true;
+        if (!finished.empty()) s->cv_done.notify_all();
+        uint32_t launches = 0;
+        for (Slot* sl : to_launch) launches += launch_query(s, *sl, sl->q);
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            for (Slot* sl : to_launch) sl->launching = false;
+            s->totals.kernel_launches += launches;
             bool any_busy = false;
             for (Slot& sl : s->slots) any_busy |= sl.q != nullptr;
-            if (s->stop && !any_busy) return true;
-            if (s->pending.empty() || s->mem_blocked || s->pause_admission) return false;
-            for (Slot& sl : s->slots)
-                if (!sl.q) return true;
-            return false;
-        });
+            if (!any_busy) s->cv_done.notify_all();   // a graph being added waits for idle slots
+        }
     }
 }
 
@@ -279,7 +311,7 @@ scan_status scan_server_create(int device, uint64_t memory_budget_bytes, uint32_
                                                 std::string(cudaGetErrorString(err)));
     }
     s->arena.reset(memory_budget_bytes);
-    s->slots.resize(max_in_flight);
+    s->slots = std::vector<Slot>(max_in_flight);   // Slot holds an atomic: built in place, never moved
     for (Slot& sl : s->slots) {
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreate(&sl.ev_start) != cudaSuccess || cudaEventCreate(&sl.ev_end) != cudaSuccess ||
@@ -310,10 +342,11 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
     }
     d->cn_valid = true;
     std::unique_lock<std::mutex> lock(s->mu);
-    // Result staging must hold the largest graph.  Growing it waits for the slots to drain
-    // (admission paused), so no copy is in flight into a buffer being replaced.
+    // Result staging must hold the largest graph.  Growing it pauses admission and waits for
+    // the slots to drain, then reallocates with the lock released (no CUDA call under it).
     bool grow = false;
     for (Slot& sl : s->slots) grow |= sl.n_cap < d->n;
+    scan_status grow_status = SCAN_OK;
     if (grow) {
         s->pause_admission = true;
         s->cv_done.wait(lock, [&] {
@@ -321,23 +354,24 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
                 if (sl.q) return false;
             return true;
         });
-    }
-    scan_status grow_status = SCAN_OK;
-    for (Slot& sl : s->slots) {
-        if (sl.n_cap >= d->n) continue;
-        if (sl.h_label) cudaFreeHost(sl.h_label);
-        if (sl.h_role) cudaFreeHost(sl.h_role);
-        sl.h_label = nullptr;
-        sl.h_role = nullptr;
-        if (cudaHostAlloc(&sl.h_label, d->n * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&sl.h_role, d->n, cudaHostAllocDefault) != cudaSuccess) {
+        lock.unlock();
+        for (Slot& sl : s->slots) {
+            if (sl.n_cap >= d->n) continue;
+            if (sl.h_label) cudaFreeHost(sl.h_label);
+            if (sl.h_role) cudaFreeHost(sl.h_role);
+            sl.h_label = nullptr;
+            sl.h_role = nullptr;
             sl.n_cap = 0;
-            grow_status = fail(SCAN_ERR_OUT_OF_MEMORY, "cannot allocate pinned result staging");
-            break;
+            if (cudaHostAlloc(&sl.h_label, d->n * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc(&sl.h_role, d->n, cudaHostAllocDefault) != cudaSuccess) {
+                grow_status = fail(SCAN_ERR_OUT_OF_MEMORY, "cannot allocate pinned result staging");
+                break;
+            }
+            sl.n_cap = d->n;
         }
-        sl.n_cap = d->n;
+        lock.lock();
+        s->pause_admission = false;
     }
-    s->pause_admission = false;
     if (grow_status != SCAN_OK) {
         lock.unlock();
         s->cv_work.notify_one();
@@ -369,6 +403,7 @@ scan_status scan_server_submit(scan_server* s, uint32_t graph_id, const char* ep
     {
         std::lock_guard<std::mutex> lock(s->mu);
         if (graph_id >= s->graphs.size()) return fail(SCAN_ERR_INVALID_ARG, "unknown graph id");
+        q->graph = s->graphs[graph_id];
         if (s->stop) return fail(SCAN_ERR_INVALID_ARG, "server is shutting down");
         q->ticket = s->next_ticket++;
         *ticket = q->ticket;

@@ -121,6 +121,17 @@ scan_status scan_graph_validate(const scan_graph* g, int check_symmetry);
 /* Copy the CSR to device `device` and keep it there (plus the lower-list orientation),
  * so later scan_run calls start with inputs resident in HBM. */
 scan_status scan_graph_upload(scan_graph* g, int device);
+/* Streamed residency for graphs above a device-memory budget: the adjacency (the only
+ * O(m) array the kernels gather from) stays in pinned, GPU-mapped host memory and is read
+ * over the host link; offsets, orientation, counts and run scratch go to the device.  Fails
+ * with SCAN_ERR_OUT_OF_MEMORY if the device part exceeds device_budget_bytes (0: no cap).
+ * Later scan_run / scan_common_neighbors calls use this copy.  This is the GB300 form of the
+ * reference's managed-memory and out-of-core variants (GPUSCAN++UVM/SCANum.cu:725-741,
+ * GPUSCAN++O/SCANoffload.cu:976-1438). */
+scan_status scan_graph_upload_streamed(scan_graph* g, int device, uint64_t device_budget_bytes,
+                                       uint64_t* device_bytes_used);
+/* Device memory held by the graph's resident copy (0 if none). */
+uint64_t scan_graph_device_bytes(const scan_graph* g);
 /* Drop the device copy (the host copy stays). */
 scan_status scan_graph_release_device(scan_graph* g);
 
@@ -156,6 +167,11 @@ scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
                      scan_predicate predicate, int32_t* out_label, uint8_t* out_role,
                      scan_stats* stats);
 
+/* Autotune the similarity stage of the resident graph (uploading it first): times task sizes
+ * x long-list thresholds and keeps the fastest for later runs.  Outputs may be NULL. */
+scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similarity_ms,
+                                uint32_t* long_words, uint64_t* target_probes);
+
 /* Exact common-neighbour count of every undirected edge, in the reference's edge order
  * (the eid / edge_u / edge_v order of scan_orient_reference): out_cn[E]. */
 scan_status scan_common_neighbors(scan_graph* g, int device, uint32_t* out_cn,
@@ -176,6 +192,32 @@ int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj,
                              const uint32_t* num_edges, const uint32_t* eid,
                              const int32_t* edge_u, const int32_t* edge_v, double eps,
                              int mu);
+
+/* ---- batched SCAN: many graphs with their own (eps, mu) in one pass ------------------
+ * No counterpart in the reference (it runs one graph per process).  The graphs become one
+ * disjoint union on the device; one set of kernels covers all of them, captured once into a
+ * CUDA graph and replayed per run.  With autotune != 0 the similarity stage's task size and
+ * long-list threshold are chosen by timing on this batch.  Results equal scan_run per graph. */
+typedef struct scan_batch scan_batch;
+
+typedef struct scan_batch_stats {
+    double ms_device;           /* the graph launch (similarity + cluster stages), CUDA events */
+    double ms_total;            /* host wall time of the call, copies and split included       */
+    uint64_t num_graphs, num_vertices, num_edges, num_cores, num_clusters;
+    uint32_t graph_kernels;     /* kernels inside the captured graph                          */
+    uint32_t long_words;        /* tuned long-list threshold (16-byte words)                  */
+    uint64_t target_probes;     /* tuned probe work per task                                  */
+    double tuned_similarity_ms; /* similarity time of the chosen setting (0 if not tuned)     */
+} scan_batch_stats;
+
+scan_status scan_batch_create(const scan_graph* const* graphs, uint32_t count, int device,
+                              int autotune, scan_batch** out);
+/* eps_decimal[i], mu[i]: graph i's parameters.  out_labels[i] (n_i entries) and out_roles[i]
+ * (may be NULL) receive graph i's result in its own vertex ids. */
+scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const int32_t* mu,
+                           scan_predicate predicate, int32_t* const* out_labels,
+                           uint8_t* const* out_roles, scan_batch_stats* stats);
+void scan_batch_free(scan_batch* b);
 
 /* ---- serving: queries on resident graphs with cached common-neighbour counts ---------
  * Serves the benchmark spec's serving pattern; the reference has no serving loop.  Each graph
