@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "ScanError", "Graph", "ScanStats", "GPUScan", "count_clusters", "library_path", "load_library",
-    "cores_noalloc", "Server", "Batch", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
+    "cores_noalloc", "Server", "Batch", "convert_edge_list", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
 ]
 
 PRED_EXACT = 0
@@ -117,6 +117,7 @@ _SIGS = {
                                    C.POINTER(C.c_uint64)]),
     "scan_gpuscan_compat": (_i32p, [C.c_int64, C.c_int64, _i32p, _u32p, _u32p, _i32p, _i32p, C.c_double, C.c_int]),
     "scan_count_clusters": (C.c_uint64, [_i32p, C.c_uint64]),
+    "scan_convert_edge_list": (C.c_int, [C.c_char_p, C.c_char_p, _u64p, _u64p]),
     "scan_eps_to_decimal": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
     "scan_graph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint32), _u64p]),
     "scan_cores_noalloc": (C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, C.c_uint64, C.c_char_p, C.c_int, C.c_int, _vp,
@@ -526,6 +527,15 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def convert_edge_list(edge_list_path, out_dir) -> tuple[int, int]:
+    """Edge-list text -> b_degree.bin / b_adj.bin (csr_convert's format); returns (n, E)."""
+    Path(out_dir).mkdir(parents=True, exist_ok=True)
+    n, e = C.c_uint64(0), C.c_uint64(0)
+    _check(load_library().scan_convert_edge_list(str(edge_list_path).encode(), str(out_dir).encode(), C.byref(n),
+                                                 C.byref(e)))
+    return n.value, e.value
 
 
 def count_clusters(label: np.ndarray) -> int:

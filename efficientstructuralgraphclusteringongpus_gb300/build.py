@@ -20,6 +20,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = BUILD / "libscan_gb300.so"
 CLI = BUILD / "gpuscan"
+CONVERT_CLI = BUILD / "scan-convert"
 
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
@@ -41,7 +42,7 @@ def _run(cmd: list[str]) -> None:
 
 def _stamp() -> str:
     h = hashlib.sha256()
-    for name in CXX_SOURCES + CU_SOURCES + HEADERS + ["cli.cpp"]:
+    for name in CXX_SOURCES + CU_SOURCES + HEADERS + ["cli.cpp", "convert_cli.cpp"]:
         h.update((CSRC / name).read_bytes())
     for hdr in sorted(INCLUDE.glob("*.h")):
         h.update(hdr.read_bytes())
@@ -55,7 +56,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     stamp_file = BUILD / "stamp"
     stamp = _stamp()
-    if not force and LIB.exists() and CLI.exists() and stamp_file.exists() and stamp_file.read_text() == stamp:
+    if (not force and LIB.exists() and CLI.exists() and CONVERT_CLI.exists() and stamp_file.exists()
+            and stamp_file.read_text() == stamp):
         return LIB
     jobs = []
     objs = []
@@ -74,8 +76,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         cuda_lib = CUDA_HOME / "targets" / f"{os.uname().machine}-linux" / "lib"
     _run(["g++", "-shared", "-o", str(LIB), *map(str, objs), f"-L{cuda_lib}", "-lcudart", "-fopenmp",
           f"-Wl,-rpath,{cuda_lib}", "-Wl,--no-undefined"])
-    _run(["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(CSRC / "cli.cpp"), "-o", str(CLI), f"-L{BUILD}",
-          "-lscan_gb300", "-Wl,-rpath,$ORIGIN"])
+    for src, exe in (("cli.cpp", CLI), ("convert_cli.cpp", CONVERT_CLI)):
+        _run(["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(CSRC / src), "-o", str(exe), f"-L{BUILD}",
+              "-lscan_gb300", "-Wl,-rpath,$ORIGIN"])
     stamp_file.write_text(stamp)
     if verbose:
         print(f"built {LIB} and {CLI}", file=sys.stderr)

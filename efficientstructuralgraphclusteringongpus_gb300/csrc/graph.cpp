@@ -591,6 +591,77 @@ scan_status scan_orient_reference(const scan_graph* g, uint32_t* eid, int32_t* e
     return SCAN_OK;
 }
 
+scan_status scan_convert_edge_list(const char* edge_list_path, const char* out_dir, uint64_t* num_vertices,
+                                   uint64_t* num_edges) {
+    clear_error();
+    if (!edge_list_path || !out_dir) return fail(SCAN_ERR_INVALID_ARG, "null path");
+    FILE* f = std::fopen(edge_list_path, "rb");
+    if (!f) return fail(SCAN_ERR_IO, std::string("cannot open ") + edge_list_path + ": " + std::strerror(errno));
+    std::unique_ptr<FILE, int (*)(FILE*)> guard(f, std::fclose);
+    std::vector<uint64_t> pairs;
+    uint64_t max_second = 0;
+    bool any = false;
+    std::vector<char> buf(1 << 20);
+    std::string carry;
+    auto parse_line = [&](const char* b, const char* e) -> bool {
+        // "# ..." comment lines are skipped; otherwise two integers.  Lines with
+        // first >= second are dropped (self-loops, and the second copy of each edge),
+        // exactly as csr_convert/EdgeListToBinsConverter.cpp:28-46 does.
+        while (b < e && (*b == ' ' || *b == '\t')) ++b;
+        if (b == e || *b == '#' || *b == '\r') return true;
+        uint64_t v[2];
+        for (int k = 0; k < 2; ++k) {
+            while (b < e && (*b == ' ' || *b == '\t' || *b == ',')) ++b;
+            if (b == e || *b < '0' || *b > '9') return false;
+            uint64_t x = 0;
+            while (b < e && *b >= '0' && *b <= '9') {
+                x = x * 10 + (uint64_t)(*b - '0');
+                if (x > 0x7FFFFFFEull) return false;
+                ++b;
+            }
+            v[k] = x;
+        }
+        if (v[0] >= v[1]) return true;
+        pairs.push_back((v[0] << 32) | v[1]);
+        if (v[1] > max_second) max_second = v[1];
+        any = true;
+        return true;
+    };
+    uint64_t line_no = 0;
+    size_t got;
+    while ((got = std::fread(buf.data(), 1, buf.size(), f)) > 0) {
+        const char* p = buf.data();
+        const char* end = p + got;
+        while (p < end) {
+            const char* nl = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+            if (!nl) { carry.append(p, end); break; }
+            ++line_no;
+            bool ok;
+            if (!carry.empty()) {
+                carry.append(p, nl);
+                ok = parse_line(carry.data(), carry.data() + carry.size());
+                carry.clear();
+            } else {
+                ok = parse_line(p, nl);
+            }
+            if (!ok) return fail(SCAN_ERR_FORMAT, "edge list line " + std::to_string(line_no) + " is not two vertex ids");
+            p = nl + 1;
+        }
+    }
+    if (!carry.empty() && !parse_line(carry.data(), carry.data() + carry.size()))
+        return fail(SCAN_ERR_FORMAT, "last edge list line is not two vertex ids");
+    if (!any) return fail(SCAN_ERR_FORMAT, "edge list has no edge with first < second");
+    const uint64_t n = max_second + 1;   // the converter's vertex count (largest second id + 1)
+    scan_graph g;
+    scan_status st = build_from_pairs(n, pairs, &g);
+    if (st) return st;
+    st = scan_graph_save(&g, out_dir);
+    if (st) return st;
+    if (num_vertices) *num_vertices = g.n;
+    if (num_edges) *num_edges = g.m / 2;
+    return SCAN_OK;
+}
+
 uint64_t scan_count_clusters(const int32_t* label, uint64_t n) {
     if (!label || n == 0) return 0;
     std::vector<uint8_t> seen(n, 0);

@@ -292,6 +292,14 @@ scan_status scan_cores_noalloc(const uint32_t* d_offsets, uint32_t n, const uint
                                uint64_t num_edges, const char* eps_decimal, int mu,
                                scan_predicate predicate, uint8_t* d_is_core, void* stream);
 
+/* Edge-list text -> <out_dir>/b_degree.bin + b_adj.bin, as csr_convert does
+ * (csr_convert/EdgeListToBinsConverter.cpp:22-121): lines starting with '#' are skipped,
+ * lines "first second" with first >= second are dropped (so each edge is taken from its
+ * first < second copy), n = largest second id + 1, lists sorted and symmetric.  Unlike the
+ * converter, repeated lines are merged (its output would fail its own loader's check). */
+scan_status scan_convert_edge_list(const char* edge_list_path, const char* out_dir,
+                                   uint64_t* num_vertices, uint64_t* num_edges);
+
 /* Number of distinct labels >= 0, as printed by the reference CLI (main.cpp:83-111). */
 uint64_t scan_count_clusters(const int32_t* label, uint64_t n);
 

@@ -5,6 +5,7 @@
   oracle/_ref/gpuscan_ref.cubin    the reference's kernels, GPUSCAN++/GPUScan.cu compiled unmodified
   oracle/_ref/libref_graph.so      the reference's host orientation, GPUSCAN++/Graph.cpp compiled
                                    unmodified plus a C shim (only on the machine holding the sources)
+  oracle/_ref/ref_convert          the reference's converter, csr_convert/EdgeListToBinsConverter.cpp
 
 The two oracle/_ref outputs are built from the reference sources where they lie and only
 when those sources are present; everything they produce stays out of version control.
@@ -28,6 +29,8 @@ ORACLE_LIB = BUILD / "liboracle.so"
 HARNESS_LIB = BUILD / "libref_harness.so"
 REF_CUBIN = REF_OUT / "gpuscan_ref.cubin"
 REF_GRAPH_LIB = REF_OUT / "libref_graph.so"
+REF_CONVERT = REF_OUT / "ref_convert"
+REFERENCE_CONVERT = Path("/root/reference/csr_convert")
 
 
 def _run(cmd: list[str]) -> None:
@@ -79,6 +82,11 @@ def build_reference() -> bool:
         _run(["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-fopenmp", "-include", "cstdint", "-include",
               "cstring", "-include", "string", f"-I{REFERENCE}", str(REFERENCE / "Graph.cpp"),
               str(HERE / "ref_graph_shim.cpp"), "-o", str(REF_GRAPH_LIB)])
+    # The reference's edge-list converter, unmodified (plain C++).
+    if (REFERENCE_CONVERT / "EdgeListToBinsConverter.cpp").exists() and _stale(
+            REF_CONVERT, REFERENCE_CONVERT / "EdgeListToBinsConverter.cpp", Path(__file__)):
+        _run(["g++", "-O2", "-std=c++14", "-include", "algorithm", "-include", "cstdint", f"-I{REFERENCE_CONVERT}",
+              str(REFERENCE_CONVERT / "EdgeListToBinsConverter.cpp"), "-o", str(REF_CONVERT)])
     return True
 
 

@@ -3,6 +3,9 @@
   --orient   (CPU; needs the reference sources, compiled by oracle/build.py into
              oracle/_ref/libref_graph.so) -> orient_<name>.npz:
              CSR + eid / Edge_u / Edge_v from GPUSCAN++/Graph.cpp:52-141 (getEidAndEdgeList).
+  --convert  (CPU; needs oracle/_ref/ref_convert, csr_convert/EdgeListToBinsConverter.cpp built from
+             the reference sources) -> convert_edges.txt + convert_b_degree.bin / convert_b_adj.bin:
+             an edge list (comments, both directions, a self-loop) and the converter's output.
   --kernels  (GPU; needs oracle/_ref/gpuscan_ref.cubin, the reference's GPUScan.cu kernels)
              -> refgpu_<name>.npz: CSR + the reference's result array for several (eps, mu),
              produced by oracle/ref_harness.cu replaying GPUScan() (GPUSCAN++/GPUScan.cu:800-1009).
@@ -55,6 +58,34 @@ def make_orient(out: Path) -> None:
         print("wrote", out / f"orient_{name}.npz")
 
 
+def convert_edge_list_text() -> str:
+    g = sg.Graph.rmat(9, 8, seed=4)
+    off, adj = g.offsets(), g.adjacency()
+    lines = ["# synthetic edge list: both directions of each edge, a self-loop, a comment"]
+    for v in range(g.n):
+        for w in adj[off[v]:off[v + 1]]:
+            lines.append(f"{v} {w}")
+    lines.insert(5, "7 7")
+    return "\n".join(lines) + "\n"
+
+
+def make_convert(out: Path) -> None:
+    import subprocess
+    import tempfile
+
+    from oracle import build as ob
+    if not ob.REF_CONVERT.exists():
+        raise SystemExit("reference converter missing (build oracle/_ref first)")
+    text = convert_edge_list_text()
+    (out / "convert_edges.txt").write_text(text)
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([str(ob.REF_CONVERT), str(out / "convert_edges.txt"), f"{tmp}/deg", f"{tmp}/adj"], check=True,
+                       stdout=subprocess.DEVNULL)
+        (out / "convert_b_degree.bin").write_bytes(Path(f"{tmp}/deg").read_bytes())
+        (out / "convert_b_adj.bin").write_bytes(Path(f"{tmp}/adj").read_bytes())
+    print("wrote", out / "convert_b_degree.bin")
+
+
 def make_kernels(out: Path) -> None:
     if not oracle.reference_kernels_available():
         raise SystemExit("reference cubin missing (build oracle/_ref first)")
@@ -73,12 +104,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--orient", action="store_true")
     ap.add_argument("--kernels", action="store_true")
+    ap.add_argument("--convert", action="store_true")
     ap.add_argument("--out", default=str(Path(__file__).resolve().parent))
     a = ap.parse_args()
     out = Path(a.out)
     out.mkdir(parents=True, exist_ok=True)
     if a.orient:
         make_orient(out)
+    if a.convert:
+        make_convert(out)
     if a.kernels:
         make_kernels(out)
 

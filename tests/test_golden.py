@@ -57,3 +57,39 @@ def test_oracle_admits_reference_gpu_output(path):
         # reference had no multi-cluster border choice to make
         if counts["multi_borders"] == 0:
             assert np.array_equal(ref, label)
+
+
+def test_converter_matches_reference_converter_output(tmp_path):
+    """scan_convert_edge_list vs the bytes the reference's converter
+    (csr_convert/EdgeListToBinsConverter.cpp) wrote for the same edge list."""
+    n, e = sg.convert_edge_list(GOLDEN / "convert_edges.txt", tmp_path / "out")
+    assert (tmp_path / "out" / "b_degree.bin").read_bytes() == (GOLDEN / "convert_b_degree.bin").read_bytes()
+    assert (tmp_path / "out" / "b_adj.bin").read_bytes() == (GOLDEN / "convert_b_adj.bin").read_bytes()
+    g = sg.Graph.load(tmp_path / "out")
+    assert (g.n, g.num_edges) == (n, e)
+
+
+def test_converter_against_live_reference(tmp_path):
+    import subprocess
+
+    from oracle import build as ob
+    if not ob.REF_CONVERT.exists():
+        pytest.skip("reference converter not built on this machine")
+    rng = np.random.default_rng(3)
+    pairs = rng.integers(0, 300, size=(2000, 2))
+    lines = ["# random"] + [f"{a} {b}" for a, b in pairs] + [f"{b} {a}" for a, b in pairs]
+    # the reference keeps duplicate lines; feed it unique ones so its output is valid
+    lines = ["# random"] + sorted(set(lines[1:]), key=lines[1:].index)
+    (tmp_path / "e.txt").write_text("\n".join(lines) + "\n")
+    subprocess.run([str(ob.REF_CONVERT), str(tmp_path / "e.txt"), str(tmp_path / "d"), str(tmp_path / "a")],
+                   check=True, stdout=subprocess.DEVNULL)
+    sg.convert_edge_list(tmp_path / "e.txt", tmp_path / "mine")
+    assert (tmp_path / "mine" / "b_degree.bin").read_bytes() == (tmp_path / "d").read_bytes()
+    assert (tmp_path / "mine" / "b_adj.bin").read_bytes() == (tmp_path / "a").read_bytes()
+
+
+def test_converter_rejects_garbage(tmp_path):
+    (tmp_path / "bad.txt").write_text("0 1\nnot numbers\n")
+    with pytest.raises(sg.ScanError) as e:
+        sg.convert_edge_list(tmp_path / "bad.txt", tmp_path / "o")
+    assert e.value.status == 3
