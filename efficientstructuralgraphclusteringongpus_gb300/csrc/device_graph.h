@@ -20,6 +20,7 @@ struct PlanParams {
     unsigned long long target_probes;          // probe work per hash-class task
     unsigned long long target_probes_bitmap;   // probe work per bitmap task
     uint32_t min_slice_edges;
+    uint32_t chunk_max;                        // pivot entries per largest-class table (<= kChunkMaxCap)
 };
 }
 

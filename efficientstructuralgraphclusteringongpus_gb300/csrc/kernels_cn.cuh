@@ -26,7 +26,8 @@ namespace scan {
 
 constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single warp
 constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
-constexpr uint32_t kChunkMax = 6144;       // max pivot entries staged by one CTA
+constexpr uint32_t kChunkMax = 6144;       // default max pivot entries staged by one CTA (load 1/4)
+constexpr uint32_t kChunkMaxCap = 12288;   // largest allowed (load 1/2 in the same table)
 // Bitmap path: the kHotBits highest-degree vertices get ids in [0, kHotBits) ("hot");
 // every other vertex x is kHotBits + x.  A pivot's hot neighbours go into a shared-memory
 // bitmap (one bit per hot id, 128 KB), the rest (its "tail") into a bucketed table.
@@ -37,6 +38,7 @@ constexpr uint32_t kBitmapMinDeg = 1024;   // pivots above this degree use the b
 constexpr int kBitmapThreads = 1024;
 __host__ __device__ constexpr uint32_t big_class_entries(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : kChunkMax; }
 __host__ __device__ constexpr uint32_t big_class_slots(int c) { return 4u * big_class_entries(c); }   // load <= 1/4
+                                                                                                   // (class 2: <= 1/2)
 
 struct CnTask {
     uint32_t v;      // pivot
@@ -171,35 +173,21 @@ __device__ __forceinline__ uint32_t probe_word(const uint4 x, uint32_t p, uint32
     return c;
 }
 
-// One list adj[b, e) streamed by the whole warp; returns this lane's hits.  Words lying
-// wholly inside [b, e) are probed without per-entry range checks; the partial first and
-// last words (at most two) are masked.
-__device__ __forceinline__ uint32_t probe_word_full(const uint4 x, const uint32_t* tab, uint32_t nb) {
-    return bucket_has(tab, nb, x.x) + bucket_has(tab, nb, x.y) + bucket_has(tab, nb, x.z) + bucket_has(tab, nb, x.w);
-}
-
+// One list adj[b, e) streamed by the whole warp; returns this lane's hits.  (Every lane
+// runs the same masked probe: measured faster than a separate unmasked interior path, whose
+// head/tail words serialise.)
 __device__ __forceinline__ uint32_t warp_probe_list(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
                                                     const uint32_t* tab, uint32_t nb, uint32_t lane) {
-    const uint32_t in_b = (b + 3u) & ~3u;          // first full word
-    const uint32_t in_e = e & ~3u;                 // end of the full words
     uint32_t c = 0;
-    if (in_b < in_e) {
-        for (uint32_t p = in_b + 4 * lane; p < in_e; p += 128 * kWordsInFlight) {
-            uint4 x[kWordsInFlight];
+    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
+        uint4 x[kWordsInFlight];
 #pragma unroll
-            for (int q = 0; q < kWordsInFlight; ++q) {
-                const uint32_t pq = p + 128 * q;
-                x[q] = pq < in_e ? __ldg(reinterpret_cast<const uint4*>(adj + pq)) : make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
-            }
-#pragma unroll
-            for (int q = 0; q < kWordsInFlight; ++q)
-                if (p + 128 * q < in_e) c += probe_word_full(x[q], tab, nb);
+        for (int q = 0; q < kWordsInFlight; ++q) {
+            const uint32_t pq = p + 128 * q;
+            x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(adj + pq)) : make_uint4(0, 0, 0, 0);
         }
-        if (lane == 0 && b < in_b) c += probe_word(__ldg(reinterpret_cast<const uint4*>(adj + (b & ~3u))), b & ~3u, b, e, tab, nb);
-        if (lane == 1 && in_e < e) c += probe_word(__ldg(reinterpret_cast<const uint4*>(adj + in_e)), in_e, b, e, tab, nb);
-    } else if (lane == 0) {                        // the list lies within at most two words
-        for (uint32_t p = b & ~3u; p < e; p += 4)
-            c += probe_word(__ldg(reinterpret_cast<const uint4*>(adj + p)), p, b, e, tab, nb);
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) c += probe_word(x[q], p + 128 * q, b, e, tab, nb);
     }
     return c;
 }
@@ -318,36 +306,19 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
     return c;
 }
 
-__device__ __forceinline__ uint32_t bitmap_word_full(const uint4 x, const uint32_t* bits, const uint32_t* tail,
-                                                     uint32_t ntb) {
-    return bitmap_probe_word(x, 0u, 0u, 4u, bits, tail, ntb);
-}
-
 __device__ __forceinline__ uint32_t warp_probe_list_bitmap(const uint32_t* __restrict__ radj, uint32_t b, uint32_t e,
                                                            const uint32_t* bits, const uint32_t* tail, uint32_t ntb,
                                                            uint32_t lane) {
-    const uint32_t in_b = (b + 3u) & ~3u;
-    const uint32_t in_e = e & ~3u;
     uint32_t c = 0;
-    if (in_b < in_e) {
-        for (uint32_t p = in_b + 4 * lane; p < in_e; p += 128 * kWordsInFlight) {
-            uint4 x[kWordsInFlight];
+    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
+        uint4 x[kWordsInFlight];
 #pragma unroll
-            for (int q = 0; q < kWordsInFlight; ++q) {
-                const uint32_t pq = p + 128 * q;
-                x[q] = pq < in_e ? __ldg(reinterpret_cast<const uint4*>(radj + pq)) : make_uint4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int q = 0; q < kWordsInFlight; ++q)
-                if (p + 128 * q < in_e) c += bitmap_word_full(x[q], bits, tail, ntb);
+        for (int q = 0; q < kWordsInFlight; ++q) {
+            const uint32_t pq = p + 128 * q;
+            x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(radj + pq)) : make_uint4(0, 0, 0, 0);
         }
-        if (lane == 0 && b < in_b)
-            c += bitmap_probe_word(__ldg(reinterpret_cast<const uint4*>(radj + (b & ~3u))), b & ~3u, b, e, bits, tail, ntb);
-        if (lane == 1 && in_e < e)
-            c += bitmap_probe_word(__ldg(reinterpret_cast<const uint4*>(radj + in_e)), in_e, b, e, bits, tail, ntb);
-    } else if (lane == 0) {
-        for (uint32_t p = b & ~3u; p < e; p += 4)
-            c += bitmap_probe_word(__ldg(reinterpret_cast<const uint4*>(radj + p)), p, b, e, bits, tail, ntb);
+#pragma unroll
+        for (int q = 0; q < kWordsInFlight; ++q) c += bitmap_probe_word(x[q], p + 128 * q, b, e, bits, tail, ntb);
     }
     return c;
 }
@@ -483,7 +454,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                 nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
                 ntask = nsl;
             } else {
-                nch = (dv + kChunkMax - 1) / kChunkMax;
+                nch = (dv + pp.chunk_max - 1) / pp.chunk_max;
                 const uint32_t ce = (dv + nch - 1) / nch;
                 cls = 1 + (ce <= big_class_entries(0) ? 0 : ce <= big_class_entries(1) ? 1 : 2);
                 unsigned long long w = work[v] / nch;   // probes per chunk (ids spread evenly)

@@ -359,6 +359,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     pp.target_probes = 1ull << 22;
     pp.target_probes_bitmap = 1ull << 23;
     pp.min_slice_edges = 64;
+    pp.chunk_max = kChunkMax;
     SCAN_TRY(plan_tasks(d.get(), pp));
 
     // Result and scratch arrays.
@@ -437,13 +438,15 @@ scan_status autotune_similarity(DeviceGraph* d, float* best_ms) {
     const PlanParams base = d->plan;
     const unsigned long long probes[] = {1ull << 20, 1ull << 22, 1ull << 24};
     const uint32_t longs[] = {16, 32, 64};
+    const uint32_t chunks[] = {kChunkMax, kChunkMaxCap};
     float best = 3.4e38f;
     PlanParams best_pp = base;
     uint32_t best_lw = d->long_words;
-    for (unsigned long long tp : probes) {
+    for (int trial = 0; trial < 6; ++trial) {
         PlanParams pp = base;
-        pp.target_probes = tp;
-        pp.target_probes_bitmap = 2 * tp;
+        pp.target_probes = probes[trial % 3];
+        pp.target_probes_bitmap = 2 * pp.target_probes;
+        pp.chunk_max = chunks[trial / 3];
         SCAN_TRY(plan_tasks(d, pp));
         for (uint32_t lw : longs) {
             d->long_words = lw;

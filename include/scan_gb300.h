@@ -168,7 +168,8 @@ scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
                      scan_stats* stats);
 
 /* Autotune the similarity stage of the resident graph (uploading it first): times task sizes
- * x long-list thresholds and keeps the fastest for later runs.  Outputs may be NULL. */
+ * x long-list thresholds x hub chunk sizes and keeps the fastest for later runs.  Outputs
+ * may be NULL. */
 scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similarity_ms,
                                 uint32_t* long_words, uint64_t* target_probes);
 
