@@ -155,7 +155,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
 //     names its list), loads it and probes its valid entries, and each edge's owner lane
 //     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
 constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
-constexpr int kWordsInFlight = 2;
+constexpr int kWordsInFlight = 4;
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
     if (hi <= lo) return 0u;
