@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--batch-only", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--batch-max-n", type=int, default=10000)
+    ap.add_argument("--reference-kernels", action="store_true",
+                    help="with --impl reference: time the reference's own GPU kernels (its cubin) instead")
     return ap.parse_args()
 
 
@@ -138,31 +140,36 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(deg: np.ndarray, E: int) -> dict:
-    """Bytes per launch of the common-neighbour stage.
+def byte_models(off: np.ndarray, adj: np.ndarray, eps: str) -> dict:
+    """Algorithmic bytes of one launch of the common-neighbour stage, from the graph alone.
 
+    prune model: a one-shot run reads only the lists of edges the degree prune leaves at
+    this eps (du + 1 >= eps^2 (dv + 1), u the lower endpoint); each such list once (4 du),
+    every pivot list staged once (4 d_v), and every edge costs its endpoint, two offsets
+    and its count (16 B) plus the zeroing of cn (4 B):  B = 4 sum_counted du + 4 sum_v d_v + 20 E.
+    (The roofline's own figure replaces 4 sum_counted du by the list words the kernels
+    report reading, which also reflects the early stop.)
+    full model: the same with every edge counted (the cached counts of the serving path).
     merge model (the per-edge figure of the survey): each edge streams both lists,
       B = sum_e [4 (du + dv) + 16] + 4 E = 4 sum_v d_v^2 + 20 E.
-    probe model (the lists this kernel must read): each edge streams the lower endpoint's
-      list once (min(du, dv)), each pivot list is staged once, plus per-edge offsets,
-      endpoint and count: B = 4 sum_e min(du, dv) + 4 sum_v d_v + 16 E.
     """
-    d = deg.astype(np.float64)
-    merge = 4.0 * float((d * d).sum()) + 20.0 * E
-    return {"merge": merge, "d2": float((d * d).sum())}
-
-
-def probe_bytes(off: np.ndarray, adj: np.ndarray) -> float:
     deg = np.diff(off).astype(np.int64)
     n = deg.size
     src = np.repeat(np.arange(n, dtype=np.int64), deg)
-    du = deg[src]
-    dv = deg[adj.astype(np.int64)]
-    # each undirected edge appears twice; count it from its higher endpoint only
-    lower = (dv < du) | ((dv == du) & (adj.astype(np.int64) < src))
-    s_min = float(dv[lower].sum())
+    a = adj.astype(np.int64)
+    ds, da = deg[src], deg[a]
+    # each undirected edge appears twice; take it at its pivot (the higher endpoint)
+    lower = (da < ds) | ((da == ds) & (a < src))
+    du, dv = da[lower].astype(np.float64), ds[lower].astype(np.float64)
     E = int(lower.sum())
-    return 4.0 * s_min + 4.0 * float(deg.sum()) + 16.0 * E
+    e = float(eps)
+    counted = ~((du + 1.0) < (dv + 1.0) * e * e)
+    staged = 4.0 * float(deg.sum())
+    d = deg.astype(np.float64)
+    return {"prune": 4.0 * float(du[counted].sum()) + staged + 20.0 * E, "fixed": staged + 20.0 * E,
+            "full": 4.0 * float(du.sum()) + staged + 20.0 * E,
+            "merge": 4.0 * float((d * d).sum()) + 20.0 * E,
+            "counted_edges": int(counted.sum())}
 
 
 def cpu_baseline(g, eps: str, mu: int, mode: int, seconds: float) -> dict:
@@ -351,12 +358,59 @@ def reference_arm(args) -> None:
     }))
 
 
+def reference_kernels_arm(args) -> None:
+    """The reference's own GPU kernels (GPUSCAN++/GPUScan.cu compiled unmodified into a cubin)
+    on this GPU, replayed by the oracle's harness in GPUScan()'s launch order
+    (GPUSCAN++/GPUScan.cu:800-1009).  value = E / summed kernel time (CUDA events); the
+    harness's host-side core/other list compaction between launches is outside it.  The host
+    preprocessing GPUScan() expects (getEidAndEdgeList, GPUSCAN++/Graph.cpp:52-141) is done
+    once, untimed.  e2e = E / wall time of the whole call (allocation, H2D, kernels, D2H)."""
+    import efficientstructuralgraphclusteringongpus_gb300 as sg
+    from oracle import oracle
+
+    line = {"impl": "reference", "metric": "similarity edges/s", "unit": "similarity edges/s"}
+    if not oracle.reference_kernels_available():
+        line["unavailable"] = "the reference's kernel cubin was not built (needs the reference sources)"
+        print(json.dumps(line))
+        return
+    g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
+    off, adj = g.offsets(), g.adjacency()
+    E = g.num_edges
+    prep = oracle.reference_gpuscan_prepare(off, adj)
+    for _ in range(args.warmup):
+        oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)
+    ms, walls = [], []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        _, k = oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)
+        walls.append(time.perf_counter() - t)
+        ms.append(k)
+    mk = float(np.mean(ms))
+    v = E / (mk * 1e-3)
+    wall = float(np.mean(walls))
+    m = int(off[-1])
+    line.update({
+        "value": v, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mk,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor, "eps": args.eps,
+                   "mu": args.mu, "predicate": "reference"},
+        "kernel_ms": [round(x, 3) for x in ms],
+        "e2e": {"value": E / wall, "unit": "similarity edges/s", "ms_per_call": wall * 1e3,
+                "h2d_bytes_per_step": 4 * (off.size + 3 * m), "d2h_bytes_per_step": 4 * g.n},
+        "note": "GPUSCAN++ kernels from its cubin, on the same GPU; summed kernel time",
+    })
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         if rank == 0:
-            reference_arm(args)
+            if args.reference_kernels:
+                reference_kernels_arm(args)
+            else:
+                reference_arm(args)
         return
     import torch
 
@@ -418,9 +472,7 @@ def main():
         e2e_matches = bool(np.array_equal(out, check))
 
     # -- roofline of the common-neighbour stage -------------------------------------------
-    deg = np.diff(off).astype(np.int64)
-    ab = algorithmic_bytes(deg, E)
-    pb = probe_bytes(off, adj)
+    bm = byte_models(off, adj, args.eps)
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     if peaks_file.exists():
         peak = float(json.loads(peaks_file.read_text())["hbm_gbs"])
@@ -428,11 +480,20 @@ def main():
     else:
         peak, peak_src = 6800.0, "fallback"
     sim_s = float(np.mean(sim_ms)) / 1e3
-    roof = {"bound": "hbm", "achieved": ab["merge"] / sim_s / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": ab["merge"] / sim_s / 1e9 / peak, "traffic": None, "peak_source": peak_src,
-            "bytes_model": "merge: 4*sum_v d_v^2 + 20E (both lists per edge)",
-            "probe_model": {"achieved": pb / sim_s / 1e9, "frac": pb / sim_s / 1e9 / peak,
-                            "bytes": pb, "definition": "4*sum_e min(du,dv) + 4*sum_v d_v + 16E"},
+
+    def gbs(b):
+        return {"achieved": b / sim_s / 1e9, "frac": b / sim_s / 1e9 / peak, "bytes": b}
+
+    words = float(np.mean([s["cn_words"] for s in stats]))
+    run_bytes = 16.0 * words + bm["fixed"]
+    roof = {"bound": "hbm", "achieved": run_bytes / sim_s / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": run_bytes / sim_s / 1e9 / peak, "traffic": None, "peak_source": peak_src,
+            "bytes": run_bytes, "list_words_read": words, "counted_edges": int(last["cn_edges_counted"]),
+            "bytes_model": "16*(list words read, reported by the kernels) + 4*sum_v d_v + 20E",
+            "prune_model": dict(gbs(bm["prune"]), counted_edges=bm["counted_edges"],
+                                definition="4*sum over edges left by the degree prune of min(du,dv) + 4*sum_v d_v + 20E"),
+            "full_model": dict(gbs(bm["full"]), definition="every edge counted (serving cache)"),
+            "merge_model": dict(gbs(bm["merge"]), definition="4*sum_v d_v^2 + 20E (both lists per edge)"),
             "kernel_ms": sim_s * 1e3}
 
     result = None

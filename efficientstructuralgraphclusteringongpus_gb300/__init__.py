@@ -50,7 +50,8 @@ class ScanStats(C.Structure):
         "num_similar_edges", "pred_disagreements", "multi_cluster_borders")] + [
         (name, C.c_double) for name in ("ms_h2d", "ms_orient", "ms_similarity", "ms_cluster", "ms_d2h", "ms_total")] + [
         ("ms_cn_kernel", C.c_double * 5), ("cn_work_items", C.c_uint64 * 5),
-        ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
+        ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32), ("cn_words", C.c_uint64),
+        ("cn_edges_counted", C.c_uint64)]
 
     def as_dict(self) -> dict:
         out = {}
@@ -106,6 +107,7 @@ _SIGS = {
     "scan_graph_release_device": (C.c_int, [_vp]),
     "scan_graph_upload_streamed": (C.c_int, [_vp, C.c_int, C.c_uint64, _u64p]),
     "scan_graph_device_bytes": (C.c_uint64, [_vp]),
+    "scan_release_cached_memory": (None, []),
     "scan_gen_rmat": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_chung_lu": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_sbm": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,

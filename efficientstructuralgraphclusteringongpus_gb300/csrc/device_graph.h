@@ -56,6 +56,7 @@ struct DeviceGraph {
     uint32_t* lo_adj = nullptr;
     uint32_t* lo_src = nullptr;
     unsigned long long* work = nullptr;
+    unsigned long long* cn_ctr = nullptr;   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;
     uint32_t nsmall = 0;
     scan::CnTask* big[scan::kNumBigClasses] = {};
@@ -75,7 +76,7 @@ struct DeviceGraph {
     RunScratch rs;                 // scratch of scan_run on this graph
     uint32_t* scratch = nullptr;   // scan tile sums, then dflags
     uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [16] long lists
-    std::vector<void*> allocs;
+    std::vector<std::pair<void*, size_t>> allocs;   // (pointer, bytes), returned to the cache on free
     uint64_t device_bytes = 0;     // device memory held by this graph
     uint32_t* adj_host = nullptr;  // streamed mode: pinned, GPU-mapped adjacency (adj points into it)
     cudaEvent_t ev[16] = {};       // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
@@ -96,7 +97,9 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
                           const uint32_t* adj_host, DeviceGraph** out, scan_stats* st,
                           bool adj_in_host_memory = false);
 // cn for every edge on d->stream.
-scan_status launch_cn(DeviceGraph* d, uint32_t* launches);
+// cn for every edge; with `prune`, edges that the degree prune rules out at that eps are
+// skipped and keep cn = 0 (a one-shot run; the result is not a reusable cache).
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune = nullptr);
 // Rebuild the similarity tasks for plan parameters pp.
 scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp);
 // Time launch_cn under a few (task size, long-list threshold) settings and keep the fastest;

@@ -101,6 +101,27 @@ __device__ __forceinline__ uint32_t bucket_has(const uint32_t* tab, uint32_t nb,
     return 0u;
 }
 
+// Degree prune of a one-shot run at a fixed eps: an edge that neither predicate can call
+// similar whatever its count (ref_f64_never and exact_never both hold) is not counted;
+// its cn stays 0, which both predicates still reject.  Off (on = 0) for the cached counts.
+struct CnPrune {
+    double eps;
+    uint64_t p, q;
+    uint32_t on;
+};
+
+__device__ __forceinline__ bool cn_pruned(uint32_t du, uint32_t dv, const CnPrune& pr) {
+    return pr.on && ref_f64_never(du, dv, pr.eps) && exact_never(du, dv, pr.p, pr.q);
+}
+
+// Early-stop threshold of an unpruned edge in a one-shot run: the least count either
+// predicate could accept.  0 (count everything) when the reference's int square of the
+// count could wrap (du + 1 > 46340, where its test is not monotone in the count).
+__device__ __forceinline__ uint32_t min_similar_count(uint32_t du, uint32_t dv, const CnPrune& pr) {
+    if (du + 1u > 46340u) return 0u;
+    return min(exact_min_count(du, dv, pr.p, pr.q), ref_min_count(du, dv, pr.eps));
+}
+
 // First position in adj[b, e) whose value is >= key (scalar, uniform across the warp).
 __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
                                                     uint32_t key) {
@@ -116,7 +137,8 @@ template <int kWarpsPerBlock>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
-           const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn) {
+           const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, CnPrune pr,
+           unsigned long long* __restrict__ ctr) {
     __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* tab = tabs[wib];
@@ -130,13 +152,21 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
         for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
         __syncwarp();
         const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
+        uint32_t words = 0, counted = 0;
         for (uint32_t k = k0; k < k1; ++k) {
             const uint32_t u = lo_adj[k];
             const uint32_t ub = off[u], ue = off[u + 1];
+            if (cn_pruned(ue - ub, e - b, pr)) continue;     // cn[k] stays 0
+            words += (ue - ub + 3u) >> 2;
+            ++counted;
             uint32_t c = 0;
             for (uint32_t j = ub + lane; j < ue; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
             c = __reduce_add_sync(0xFFFFFFFFu, c);
             if (lane == 0) cn[k] = c;
+        }
+        if (lane == 0 && counted) {
+            atomicAdd(&ctr[0], (unsigned long long)words);
+            atomicAdd(&ctr[1], (unsigned long long)counted);
         }
         __syncwarp();
     }
@@ -155,7 +185,8 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
 //     names its list), loads it and probes its valid entries, and each edge's owner lane
 //     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
 constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
-constexpr int kWordsInFlight = 4;
+constexpr int kWordsInFlight = 2;        // hash kernel (48+ registers would cost occupancy)
+constexpr int kWordsInFlightBitmap = 4;  // bitmap kernel (one CTA per SM: registers to spare)
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
     if (hi <= lo) return 0u;
@@ -173,28 +204,141 @@ __device__ __forceinline__ uint32_t probe_word(const uint4 x, uint32_t p, uint32
     return c;
 }
 
-// One list adj[b, e) streamed by the whole warp; returns this lane's hits.  (Every lane
-// runs the same masked probe: measured faster than a separate unmasked interior path, whose
-// head/tail words serialise.)
-__device__ __forceinline__ uint32_t warp_probe_list(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e,
-                                                    const uint32_t* tab, uint32_t nb, uint32_t lane) {
-    uint32_t c = 0;
-    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
-        uint4 x[kWordsInFlight];
+// Entries of a list of du that must be examined, given h hits so far, before the early
+// stop can decide it: past du - tlo + h, hits + unexamined entries < tlo.  du when tlo = 0.
+__device__ __forceinline__ uint32_t needed_entries(uint32_t du, uint32_t tlo, uint32_t h) {
+    if (tlo == 0) return du;
+    const int64_t need = (int64_t)du - (int64_t)tlo + (int64_t)h + 1;
+    return need <= 0 ? 0u : need >= (int64_t)du ? du : (uint32_t)need;
+}
+
+// One list adj[b, e) streamed by the whole warp, W words in flight per lane; returns the
+// warp's total (the same in every lane).  With tlo > 0 it stops once the list is decided
+// (see needed_entries).  Every lane runs the same masked probe: measured faster than a
+// separate unmasked interior path, whose head and tail words serialise.
+template <int W, typename Probe>
+__device__ __forceinline__ uint32_t warp_list(const uint32_t* __restrict__ adj, uint32_t b, uint32_t e, uint32_t tlo,
+                                              uint32_t lane, uint32_t& words, Probe probe) {
+    uint32_t h = 0;
+    for (uint32_t base = b & ~3u; base < e; base += 128u * W) {
+        words += min(32u * W, (e - base + 3u) >> 2);
+        uint4 x[W];
 #pragma unroll
-        for (int q = 0; q < kWordsInFlight; ++q) {
-            const uint32_t pq = p + 128 * q;
+        for (int q = 0; q < W; ++q) {
+            const uint32_t pq = base + 4u * lane + 128u * q;
             x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(adj + pq)) : make_uint4(0, 0, 0, 0);
         }
+        uint32_t c = 0;
 #pragma unroll
-        for (int q = 0; q < kWordsInFlight; ++q) c += probe_word(x[q], p + 128 * q, b, e, tab, nb);
+        for (int q = 0; q < W; ++q) c += probe(x[q], base + 4u * lane + 128u * q, b, e);
+        h += __reduce_add_sync(0xFFFFFFFFu, c);
+        if (tlo && min(e, base + 128u * W) - b >= needed_entries(e - b, tlo, h)) break;
     }
-    return c;
+    return h;
+}
+
+// The short lists of a batch as one stream of 16-byte words.  Lane i's list covers words
+// [excl_i, incl_i) of the stream; each round every lane takes kShortRounds words (a
+// binary search over the inclusive prefixes names each word's list), issues their loads
+// together, probes the valid entries, and the hits are credited to the owning lanes from
+// three ballots of the per-word counts (0..4).  Returns this lane's own count.
+constexpr int kShortRounds = 1;   // measured: 2 costs more in registers than it gains
+
+template <typename Probe>
+__device__ __forceinline__ uint32_t short_stream(const uint32_t* __restrict__ adj, uint32_t lane, uint32_t wa,
+                                                 uint32_t ub, uint32_t ue, uint32_t incl, uint32_t excl,
+                                                 uint32_t total, Probe probe) {
+    uint32_t cnt = 0;
+    for (uint32_t base = 0; base < total; base += 32u * kShortRounds) {
+        uint4 x[kShortRounds];
+        uint32_t pw[kShortRounds], lbw[kShortRounds], lew[kShortRounds];
+#pragma unroll
+        for (int r = 0; r < kShortRounds; ++r) {
+            const uint32_t y = base + 32u * r + lane;
+            uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + st - 1);
+                if (pj <= y) j += st;
+            }
+            j &= 31u;
+            const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
+            const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
+            lbw[r] = __shfl_sync(0xFFFFFFFFu, ub, j);
+            lew[r] = __shfl_sync(0xFFFFFFFFu, ue, j);
+            pw[r] = aj + 4u * (y - ej);
+            x[r] = y < total ? __ldg(reinterpret_cast<const uint4*>(adj + pw[r])) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int r = 0; r < kShortRounds; ++r) {
+            const uint32_t y0 = base + 32u * r;
+            const uint32_t h = (y0 + lane < total) ? probe(x[r], pw[r], lbw[r], lew[r]) : 0u;
+            const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
+            const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
+            const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
+            const int lo = (int)min(max((int64_t)excl - (int64_t)y0, (int64_t)0), (int64_t)32);
+            const int hi = (int)min(max((int64_t)incl - (int64_t)y0, (int64_t)0), (int64_t)32);
+            const uint32_t m = lane_range_mask(lo, hi);
+            cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+        }
+    }
+    return cnt;
+}
+
+// Counts for one batch of 32 edges; lane i holds list adj[ub, ue) of its lower endpoint
+// (ue = ub for a pruned edge) and tlo, the early-stop threshold (0: count everything).
+// Lists of at least long_words words of their needed prefix go to warp_list one at a
+// time; the rest are streamed together by short_stream in phases: first each list's
+// needed prefix at zero hits, then the extension its hits require, until every list is
+// complete or decided.  Returns lane i's count (partial when decided early); adds the
+// 16-byte words the warp read to `words` (the same in every lane).
+template <int W, typename Probe>
+__device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj, uint32_t lane, uint32_t ub,
+                                                uint32_t ue, uint32_t tlo, uint32_t long_words, uint32_t& words,
+                                                Probe probe) {
+    const uint32_t du = ue - ub;
+    uint32_t end = ub + needed_entries(du, tlo, 0);
+    const uint32_t nwords = end > ub ? (((end + 3u) & ~3u) - (ub & ~3u)) >> 2 : 0u;
+    uint32_t cnt = 0;
+    uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= long_words);
+    while (longs) {
+        const int j = __ffs(longs) - 1;
+        longs &= longs - 1;
+        const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
+        const uint32_t t = __shfl_sync(0xFFFFFFFFu, tlo, j);
+        const uint32_t c = warp_list<W>(adj, b, e, t, lane, words, probe);
+        if ((int)lane == j) cnt = c;
+    }
+    const bool done_long = nwords >= long_words;          // counted by the warp above
+    uint32_t cur = ub;
+    if (done_long) end = ub;
+    for (;;) {
+        const uint32_t wa = cur & ~3u;
+        const uint32_t sw = end > cur ? (((end + 3u) & ~3u) - wa) >> 2 : 0u;
+        if (__ballot_sync(0xFFFFFFFFu, sw != 0) == 0) break;
+        uint32_t incl = sw;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+            if ((int)lane >= s) incl += y;
+        }
+        const uint32_t excl = incl - sw;
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        words += total;
+        cnt += short_stream(adj, lane, wa, cur, end, incl, excl, total, probe);
+        // the next phase: what the hits found so far require (at least 8 words more)
+        const uint32_t need = needed_entries(du, tlo, cnt);
+        const uint32_t next = (!done_long && ub + need > end) ? min(ue, max(ub + need, end + 32u)) : end;
+        cur = end;
+        end = next;
+    }
+    return cnt;
 }
 
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                         const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words) {
+                         const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
+                         CnPrune pr, unsigned long long* __restrict__ ctr) {
     extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch;
     const uint32_t lane = threadIdx.x & 31;
@@ -218,65 +362,32 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
             const uint32_t k = kb + lane;
             const bool valid = k < tk.e1;
             uint32_t ub = 0, ue = 0;
+            bool counted = false;
             if (valid) {
                 const uint32_t u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
-                if (tk.chunked) {
+                if (cn_pruned(ue - ub, ve - vb, pr)) ue = ub;
+                counted = ue > ub && tk.cb == vb;               // once per edge: in its first chunk
+                if (tk.chunked && ue > ub) {
                     if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
                     if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
                 }
             }
-            const uint32_t wa = ub & ~3u;                                 // first word (entry index)
-            const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
-            uint32_t cnt = 0;
-            // long lists: the whole warp, one list at a time
-            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= long_words);
-            while (longs) {
-                const int j = __ffs(longs) - 1;
-                longs &= longs - 1;
-                const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
-                const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, warp_probe_list(adj, b, e, tab, nb, lane));
-                if ((int)lane == j) cnt = c;
-            }
-            // short lists: one stream of words
-            const uint32_t sw = nwords < long_words ? nwords : 0u;
-            uint32_t incl = sw;
-#pragma unroll
-            for (int s = 1; s < 32; s <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
-                if ((int)lane >= s) incl += y;
-            }
-            const uint32_t excl = incl - sw;
-            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            for (uint32_t base = 0; base < total; base += 32) {
-                const uint32_t y = base + lane;
-                uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
-#pragma unroll
-                for (int s = 16; s > 0; s >>= 1) {
-                    const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
-                    if (pj <= y) j += s;
-                }
-                j &= 31u;
-                const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
-                const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
-                const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, j);
-                const uint32_t le = __shfl_sync(0xFFFFFFFFu, ue, j);
-                uint32_t h = 0;
-                if (y < total) {
-                    const uint32_t p = aj + 4u * (y - ej);
-                    h = probe_word(__ldg(reinterpret_cast<const uint4*>(adj + p)), p, lb, le, tab, nb);
-                }
-                const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
-                const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
-                const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
-                const int lo = (int)min(max((int64_t)excl - (int64_t)base, (int64_t)0), (int64_t)32);
-                const int hi = (int)min(max((int64_t)incl - (int64_t)base, (int64_t)0), (int64_t)32);
-                const uint32_t m = lane_range_mask(lo, hi);
-                cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? min_similar_count(ue - ub, ve - vb, pr) : 0u;
+            uint32_t words = 0;
+            const uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
+                                                             [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
+                                                                 return probe_word(x, p, lb, le, tab, nb);
+                                                             });
+            const uint32_t nc = __popc(__ballot_sync(0xFFFFFFFFu, counted));
+            if (lane == 0 && (words | nc)) {
+                atomicAdd(&ctr[0], (unsigned long long)words);
+                atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) {
-                if (tk.chunked) atomicAdd(&cn[k], cnt); else cn[k] = cnt;
+                if (!tk.chunked) cn[k] = cnt;
+                else if (cnt) atomicAdd(&cn[k], cnt);           // cn was zeroed before the launch
             }
         }
         __syncthreads();
@@ -306,28 +417,11 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
     return c;
 }
 
-__device__ __forceinline__ uint32_t warp_probe_list_bitmap(const uint32_t* __restrict__ radj, uint32_t b, uint32_t e,
-                                                           const uint32_t* bits, const uint32_t* tail, uint32_t ntb,
-                                                           uint32_t lane) {
-    uint32_t c = 0;
-    for (uint32_t p = (b & ~3u) + 4 * lane; p < e; p += 128 * kWordsInFlight) {
-        uint4 x[kWordsInFlight];
-#pragma unroll
-        for (int q = 0; q < kWordsInFlight; ++q) {
-            const uint32_t pq = p + 128 * q;
-            x[q] = pq < e ? __ldg(reinterpret_cast<const uint4*>(radj + pq)) : make_uint4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int q = 0; q < kWordsInFlight; ++q) c += bitmap_probe_word(x[q], p + 128 * q, b, e, bits, tail, ntb);
-    }
-    return c;
-}
-
 // task.cb carries the pivot's tail size.
 __global__ void __launch_bounds__(kBitmapThreads, 1)
 k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn,
-            uint32_t long_words) {
+            uint32_t long_words, CnPrune pr, unsigned long long* __restrict__ ctr) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* bits = smem;                              // kHotBits / 32 words
     uint32_t* tail = smem + kHotBits / 32;              // kTailSlots words
@@ -363,53 +457,19 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* _
                 const uint32_t u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
+                if (cn_pruned(ue - ub, ve - vb, pr)) ue = ub;
             }
-            const uint32_t wa = ub & ~3u;
-            const uint32_t nwords = ue > ub ? (((ue + 3u) & ~3u) - wa) >> 2 : 0u;
-            uint32_t cnt = 0;
-            uint32_t longs = __ballot_sync(0xFFFFFFFFu, nwords >= long_words);
-            while (longs) {
-                const int j = __ffs(longs) - 1;
-                longs &= longs - 1;
-                const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
-                const uint32_t c =
-                    __reduce_add_sync(0xFFFFFFFFu, warp_probe_list_bitmap(radj, b, e, bits, tail, ntb, lane));
-                if ((int)lane == j) cnt = c;
-            }
-            const uint32_t sw = nwords < long_words ? nwords : 0u;
-            uint32_t incl = sw;
-#pragma unroll
-            for (int s = 1; s < 32; s <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
-                if ((int)lane >= s) incl += y;
-            }
-            const uint32_t excl = incl - sw;
-            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            for (uint32_t base = 0; base < total; base += 32) {
-                const uint32_t y = base + lane;
-                uint32_t j = 0;
-#pragma unroll
-                for (int s = 16; s > 0; s >>= 1) {
-                    const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + s - 1);
-                    if (pj <= y) j += s;
-                }
-                j &= 31u;
-                const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
-                const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
-                const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, j);
-                const uint32_t le = __shfl_sync(0xFFFFFFFFu, ue, j);
-                uint32_t h = 0;
-                if (y < total) {
-                    const uint32_t p = aj + 4u * (y - ej);
-                    h = bitmap_probe_word(__ldg(reinterpret_cast<const uint4*>(radj + p)), p, lb, le, bits, tail, ntb);
-                }
-                const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
-                const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
-                const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
-                const int lo = (int)min(max((int64_t)excl - (int64_t)base, (int64_t)0), (int64_t)32);
-                const int hi = (int)min(max((int64_t)incl - (int64_t)base, (int64_t)0), (int64_t)32);
-                const uint32_t m = lane_range_mask(lo, hi);
-                cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+            const uint32_t tlo = (pr.on && ue > ub) ? min_similar_count(ue - ub, ve - vb, pr) : 0u;
+            uint32_t words = 0;
+            const uint32_t cnt = count_batch<kWordsInFlightBitmap>(radj, lane, ub, ue, tlo, long_words, words,
+                                                                   [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
+                                                                       return bitmap_probe_word(x, p, lb, le, bits,
+                                                                                                tail, ntb);
+                                                                   });
+            const uint32_t nc = __popc(__ballot_sync(0xFFFFFFFFu, ue > ub));
+            if (lane == 0 && (words | nc)) {
+                atomicAdd(&ctr[0], (unsigned long long)words);
+                atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
         }

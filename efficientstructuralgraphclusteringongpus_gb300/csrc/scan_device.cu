@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -95,13 +96,56 @@ using namespace scan;
 
 namespace scan {
 
+// Device-memory cache: buffers of freed resident graphs are kept per device and handed to
+// later uploads of similar size instead of cudaFree + cudaMalloc (cudaFree synchronises
+// the whole device; both cost milliseconds at GB sizes).  At most kCacheCap bytes per
+// device are kept; scan_release_cached_memory() frees them.
+constexpr size_t kCacheCap = 32ull << 30;
+static std::mutex g_cache_mu;
+static std::multimap<size_t, void*> g_cache[64];
+static size_t g_cache_bytes[64] = {};
+
+static void* cache_take(int dev, size_t bytes, size_t* actual) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    auto it = g_cache[dev].lower_bound(bytes);
+    if (it == g_cache[dev].end() || it->first > 2 * bytes + (1 << 20)) return nullptr;   // avoid large waste
+    void* p = it->second;
+    *actual = it->first;
+    g_cache_bytes[dev] -= it->first;
+    g_cache[dev].erase(it);
+    return p;
+}
+
+extern "C" void scan_release_cached_memory(void) {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    int prev = -1;
+    cudaGetDevice(&prev);
+    for (int dev = 0; dev < 64; ++dev) {
+        if (g_cache[dev].empty()) continue;
+        cudaSetDevice(dev);
+        for (auto& kv : g_cache[dev]) cudaFree(kv.second);
+        g_cache[dev].clear();
+        g_cache_bytes[dev] = 0;
+    }
+    if (prev >= 0) cudaSetDevice(prev);
+}
+
+static void cache_give(int dev, void* p, size_t bytes) {
+    if (dev < 0 || dev >= 64) { cudaFree(p); return; }
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    if (g_cache_bytes[dev] + bytes > kCacheCap) { cudaFree(p); return; }
+    g_cache[dev].emplace(bytes, p);
+    g_cache_bytes[dev] += bytes;
+}
+
 void device_graph_free(DeviceGraph* d) {
     if (!d) return;
     int prev = -1;
     cudaGetDevice(&prev);
     if (d->device >= 0) cudaSetDevice(d->device);
     if (d->stream) cudaStreamSynchronize(d->stream);
-    for (void* p : d->allocs) cudaFree(p);
+    for (auto& a : d->allocs) cache_give(d->device, a.first, a.second);
     if (d->adj_host) cudaFreeHost(d->adj_host);
     for (auto& e : d->ev)
         if (e) cudaEventDestroy(e);
@@ -112,15 +156,26 @@ void device_graph_free(DeviceGraph* d) {
 
 template <typename T>
 static scan_status dalloc(DeviceGraph* d, T** p, uint64_t count) {
-    void* q = nullptr;
-    cudaError_t err = cudaMalloc(&q, std::max<uint64_t>(count, 1) * sizeof(T));
-    if (err != cudaSuccess) {
-        cudaGetLastError();
-        return fail(SCAN_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(count * sizeof(T)) +
-                                                " bytes failed: " + cudaGetErrorString(err));
+    const size_t want = std::max<uint64_t>(count, 1) * sizeof(T);
+    const size_t bytes = (want + 255) & ~size_t(255);
+    size_t got = bytes;                    // a cached block may be larger: keep its real size
+    void* q = cache_take(d->device, bytes, &got);
+    if (!q) {
+        cudaError_t err = cudaMalloc(&q, bytes);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            // return cached blocks to the driver and try once more
+            scan_release_cached_memory();
+            err = cudaMalloc(&q, bytes);
+        }
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SCAN_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(bytes) +
+                                                    " bytes failed: " + cudaGetErrorString(err));
+        }
     }
-    d->allocs.push_back(q);
-    d->device_bytes += std::max<uint64_t>(count, 1) * sizeof(T);
+    d->allocs.emplace_back(q, got);
+    d->device_bytes += bytes;
     *p = static_cast<T*>(q);
     return SCAN_OK;
 }
@@ -302,11 +357,13 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
 
     // Hot ids for the bitmap path: the kHotBits highest-degree vertices (by degree bin).
-    // SCAN_GB300_BITMAP=on|off overrides the default ("auto": on when every vertex with an
-    // edge gets a hot id, so no pivot has a tail -- measured faster there; with tails the
-    // hash classes are kept).
+    // On by default wherever it applies: its pivots are never split, so the early stop of
+    // one-shot runs reaches the hubs too (R-MAT s22, eps 0.5: 36.5 ms against 46.9 ms for
+    // the hash classes; full counts for the cache: 66.9 against 62.8 ms).
+    // SCAN_GB300_BITMAP=off keeps the hash classes only; "tails-free" turns it on only when
+    // every vertex with an edge gets a hot id.
     const char* knob = std::getenv("SCAN_GB300_BITMAP");
-    const int mode = knob && !std::strcmp(knob, "on") ? 1 : knob && !std::strcmp(knob, "off") ? 0 : 2;
+    const int mode = knob && !std::strcmp(knob, "off") ? 0 : knob && !std::strcmp(knob, "tails-free") ? 2 : 1;
     bool bitmap_path = mode != 0 && n + kHotBits < 0xFFFFFFF0ull && m > 0 && !adj_in_host_memory;
     uint32_t* hist = nullptr;
     std::vector<uint32_t> h(kDegBins, 0);
@@ -364,6 +421,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 
     // Result and scratch arrays.
     SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
+    SCAN_TRY(dalloc(d.get(), &d->cn_ctr, 2));
     uint8_t* rs_mem = nullptr;
     SCAN_TRY(dalloc(d.get(), &rs_mem, run_scratch_bytes(d->n, d->E)));
     run_scratch_bind(&d->rs, rs_mem, d->n, d->E);
@@ -384,14 +442,17 @@ static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class 
                                                 // so capturing launch_cn into a graph queries nothing)
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
-scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune) {
     cudaStream_t s = d->stream;
+    CnPrune pr{0.0, 0, 1, 0u};
+    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u};
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
     SCAN_CUDA(cudaEventRecord(d->ev[7], s));
     if (d->nsmall) {
         constexpr int kWpb = 8;
         k_cn_small<kWpb><<<grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16), kWpb * 32, 0, s>>>(
-            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn);
+            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, pr, d->cn_ctr);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
@@ -412,7 +473,8 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
             }
             const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
             k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off,
-                                                            d->adj, d->lo_adj, d->cn, d->long_words);
+                                                            d->adj, d->lo_adj, d->cn, d->long_words, pr,
+                                                            d->cn_ctr);
             ++*launches;
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
@@ -425,7 +487,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches) {
         }
         const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
         k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->off, d->radj, d->lo_adj, d->cn,
-                                                                  d->long_words);
+                                                                  d->long_words, pr, d->cn_ctr);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
@@ -528,7 +590,8 @@ static scan_status ensure_device(scan_graph* g, int device, scan_stats* st) {
 }
 
 // Full run on a resident graph: cn (unless cached and reuse_cn), then the cluster stages,
-// then D2H of labels/roles.
+// then D2H of labels/roles.  Counts computed here skip the edges the degree prune rules
+// out at this eps, so they do not fill the cache: cn_valid is left false.
 static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bool reuse_cn, int32_t* out_label,
                                 uint8_t* out_role, scan_stats* st) {
     std::lock_guard<std::mutex> lock(d->mu);
@@ -537,7 +600,11 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
     uint32_t launches = 0;
     SCAN_CUDA(cudaEventRecord(d->ev[3], s));
     d->cn_valid_before = d->cn_valid;
-    if (!(reuse_cn && d->cn_valid)) SCAN_TRY(launch_cn(d, &launches));
+    const bool count = !(reuse_cn && d->cn_valid);
+    if (count) {
+        d->cn_valid = false;
+        SCAN_TRY(launch_cn(d, &launches, &pp));
+    }
     SCAN_CUDA(cudaEventRecord(d->ev[4], s));
     SCAN_TRY(launch_cluster(d, d->rs, s, pp, mu, &launches));
     SCAN_CUDA(cudaEventRecord(d->ev[5], s));
@@ -546,11 +613,12 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
     if (out_label) SCAN_CUDA(cudaMemcpyAsync(out_label, d->rs.label, d->n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     if (out_role) SCAN_CUDA(cudaMemcpyAsync(out_role, d->rs.role, d->n, cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaMemcpyAsync(&hc, d->rs.ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    unsigned long long cn_ctr[2] = {0, 0};
+    if (count) SCAN_CUDA(cudaMemcpyAsync(cn_ctr, d->cn_ctr, sizeof(cn_ctr), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaMemcpyAsync(&last_round, d->rs.jump_flags + jump_rounds(d->n) - 1, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaEventRecord(d->ev[6], s));
     SCAN_CUDA(cudaEventSynchronize(d->ev[6]));
-    d->cn_valid = true;
     if (hc.error_flags) return fail(SCAN_ERR_DEVICE, "union-find exceeded its iteration limit");
     if (last_round) return fail(SCAN_ERR_DEVICE, "union-find flattening did not converge");
     if (st) {
@@ -568,7 +636,11 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
         st->ms_cluster = ev_ms(d->ev[4], d->ev[5]);
         st->ms_d2h = ev_ms(d->ev[5], d->ev[6]);
         st->ms_total = ev_ms(d->ev[3], d->ev[6]);
-        if (!(reuse_cn && d->cn_valid_before)) cn_kernel_times(d, st);
+        if (count) {
+            cn_kernel_times(d, st);
+            st->cn_words = cn_ctr[0];
+            st->cn_edges_counted = cn_ctr[1];
+        }
         st->kernel_launches += launches;
     }
     return SCAN_OK;

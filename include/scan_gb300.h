@@ -86,6 +86,10 @@ typedef struct scan_stats {
     uint64_t cn_work_items[5];  /* pivots (small class) or tasks (the others) of each           */
     uint32_t kernel_launches;   /* kernels this library launched for the run                  */
     uint32_t reserved;
+    uint64_t cn_words;          /* 16-byte list words the similarity kernels read (0 when the
+                                   cached counts were used)                                  */
+    uint64_t cn_edges_counted;  /* edges whose lower list was read: all of them for the cached
+                                   counts, those the degree prune leaves in a one-shot run   */
 } scan_stats;
 
 /* ---- errors ------------------------------------------------------------------------- */
@@ -134,6 +138,9 @@ scan_status scan_graph_upload_streamed(scan_graph* g, int device, uint64_t devic
 uint64_t scan_graph_device_bytes(const scan_graph* g);
 /* Drop the device copy (the host copy stays). */
 scan_status scan_graph_release_device(scan_graph* g);
+/* Device buffers of freed graphs are cached per device (up to 32 GiB) and reused by later
+ * uploads; this returns them to the driver. */
+void scan_release_cached_memory(void);
 
 /* ---- generators (deterministic for a seed on every platform) ------------------------ */
 /* R-MAT: 2^scale vertices, edge_factor*2^scale sampled pairs with quadrant probabilities

@@ -167,7 +167,16 @@ def reference_kernels_available() -> bool:
     return _build.REF_CUBIN.exists()
 
 
-def reference_gpuscan(off, adj, eps: float, mu: int):
+def reference_gpuscan_prepare(off, adj):
+    """The host inputs GPUScan() takes (GPUSCAN++/main.cpp:52-56): uint32 offsets, int32
+    adjacency, eid and the oriented edge list, computed once so repeated calls can be timed."""
+    off64, adj32 = _csr(off, adj)
+    eu, ev = orient(off64, adj32)
+    return {"off32": off64.astype(np.uint32), "adj": adj32.astype(np.int32), "eid": eid(off64, adj32),
+            "eu": eu.astype(np.int32), "ev": ev.astype(np.int32), "n": off64.size - 1, "m": int(off64[-1])}
+
+
+def reference_gpuscan(off, adj, eps: float, mu: int, prepared=None):
     """Run the reference's kernels (its cubin) on device 0; returns (role array, kernel ms)."""
     global _harness
     if _harness is None:
@@ -177,17 +186,12 @@ def reference_gpuscan(off, adj, eps: float, mu: int):
                                   C.c_int, _i32p, C.POINTER(C.c_float)]
         L.ref_harness_error.restype = C.c_char_p
         _harness = L
-    off64, adj32 = _csr(off, adj)
-    n = off64.size - 1
-    m = int(off64[-1])
-    e = eid(off64, adj32)
-    eu, ev = orient(off64, adj32)
-    off32 = off64.astype(np.uint32)
-    a = adj32.astype(np.int32)
+    p = prepared if prepared is not None else reference_gpuscan_prepare(off, adj)
+    n, m = p["n"], p["m"]
     out = np.zeros(n, np.int32)
     ms = C.c_float(0)
-    if _harness.ref_gpuscan(str(_build.REF_CUBIN).encode(), n, m, _p(off32, C.c_uint32), _p(a, C.c_int32),
-                            _p(e, C.c_uint32), _p(eu.astype(np.int32), C.c_int32), _p(ev.astype(np.int32), C.c_int32),
+    if _harness.ref_gpuscan(str(_build.REF_CUBIN).encode(), n, m, _p(p["off32"], C.c_uint32), _p(p["adj"], C.c_int32),
+                            _p(p["eid"], C.c_uint32), _p(p["eu"], C.c_int32), _p(p["ev"], C.c_int32),
                             float(eps), int(mu), _p(out, C.c_int32), C.byref(ms)) != 0:
         raise RuntimeError("reference harness: " + _harness.ref_harness_error().decode())
     return out, ms.value

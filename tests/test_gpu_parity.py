@@ -101,13 +101,63 @@ def test_isolated_and_empty_edges():
 
 
 # ---- generated graphs -------------------------------------------------------------------
+# By default pivots above degree 1024 take the bitmap kernel; "off" forces the hash-table
+# classes and the chunked hub path on the same graphs.
+@pytest.fixture(params=["default", "off"])
+def bitmap(request, monkeypatch):
+    if request.param == "default":
+        monkeypatch.delenv("SCAN_GB300_BITMAP", raising=False)
+    else:
+        monkeypatch.setenv("SCAN_GB300_BITMAP", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("scale,seed", [(8, 1), (10, 2), (12, 3), (14, 4)])
 @pytest.mark.parametrize("eps", ["0.2", "0.4", "0.5", "0.6", "0.8"])
 @pytest.mark.parametrize("mu", [2, 5, 10])
-def test_rmat_both_modes(scale, seed, eps, mu):
+def test_rmat_both_modes(scale, seed, eps, mu, bitmap):
     g = sg.Graph.rmat(scale, 16, seed=seed)
     assert_same_as_oracle(g, eps, mu, EXACT)
     assert_same_as_oracle(g, eps, mu, REF)
+
+
+@pytest.mark.parametrize("eps", ["0.05", "0.3", "0.5", "0.7"])
+def test_rmat16_chunked_hubs_both_modes(eps, bitmap):
+    """R-MAT scale 16 has pivots above the 6144-entry chunk: with the bitmap off they are
+    split into id-range chunks."""
+    g = sg.Graph.rmat(16, 16, seed=3)
+    assert g.max_degree > 6144
+    assert_same_as_oracle(g, eps, 3, EXACT)
+    assert_same_as_oracle(g, eps, 3, REF)
+
+
+@pytest.mark.parametrize("leaves", [46337, 46338, 46339, 50000, 70000])
+def test_twin_hubs_count_square_wrap(leaves, bitmap):
+    """Two adjacent hubs sharing every leaf: T = leaves.  Past T + 2 = 46340 the reference's
+    int square wraps and ref-f64 stops calling the edge similar; exact does not."""
+    edges = [(0, 1)] + [(0, 2 + i) for i in range(leaves)] + [(1, 2 + i) for i in range(leaves)]
+    g = sg.Graph.from_edges(leaves + 2, edges)
+    for eps in ("0.5", "0.99", "1"):
+        assert_same_as_oracle(g, eps, 2, EXACT)
+        assert_same_as_oracle(g, eps, 2, REF)
+
+
+@pytest.mark.parametrize("knob", ["default", "tails-free"])
+def test_bitmap_with_tails_matches_oracle(knob, monkeypatch):
+    """More non-isolated vertices than hot ids: the bitmap kernel keeps the rest of each
+    pivot's list (its tail) in the shared-memory table ("tails-free" keeps such graphs on
+    the hash classes)."""
+    if knob == "default":
+        monkeypatch.delenv("SCAN_GB300_BITMAP", raising=False)
+    else:
+        monkeypatch.setenv("SCAN_GB300_BITMAP", knob)
+    g = sg.Graph.chung_lu(1_300_000, 2.1, 6_000_000, 20000, seed=12)
+    assert (np.diff(g.offsets()) > 0).sum() > (1 << 20)
+    for eps, mu in (("0.3", 3), ("0.5", 5)):
+        assert_same_as_oracle(g, eps, mu, EXACT)
+        assert_same_as_oracle(g, eps, mu, REF)
+    cn, _ = g.common_neighbors()
+    assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
 
 
 def test_rmat16_reference_config():
@@ -126,7 +176,7 @@ def test_rmat16_reference_config():
     lambda: star(),
     lambda: wheel(20000),                                            # one pivot in several chunks
 ])
-def test_common_neighbors_exact(make):
+def test_common_neighbors_exact(make, bitmap):
     g = make()
     cn, st = g.common_neighbors()
     ref = oracle.common_neighbors(g.offsets(), g.adjacency())
@@ -136,7 +186,7 @@ def test_common_neighbors_exact(make):
     assert st["ms_similarity"] > 0
 
 
-def test_wheel_hub_pipeline():
+def test_wheel_hub_pipeline(bitmap):
     g = wheel(20000)
     for eps in ("0.01", "0.3"):
         assert_same_as_oracle(g, eps, 2, EXACT)
@@ -150,7 +200,7 @@ def test_triangle_strip_one_long_cluster(n):
     assert res.stats["num_clusters"] == 1 and (res.label == 0).all()
 
 
-def test_chunked_hub_pipeline():
+def test_chunked_hub_pipeline(bitmap):
     g = sg.Graph.chung_lu(60000, 2.1, 400000, 30000, seed=5)
     assert g.max_degree > 6144          # above the per-CTA chunk: the hub is split
     for eps in ("0.1", "0.3"):
@@ -158,7 +208,18 @@ def test_chunked_hub_pipeline():
         assert_same_as_oracle(g, eps, 3, REF)
 
 
-def test_sbm_pipeline():
+@pytest.mark.parametrize("eps", ["0.12", "0.15", "0.18", "0.2", "0.22", "0.25"])
+def test_sbm_dense_blocks_near_threshold(eps, bitmap):
+    """Blocks of 2,000 at p_in = 0.2: lists of ~400 entries (whole-warp streaming) and
+    intra-block similarities near 0.2, so many edges are decided close to the early-stop
+    threshold."""
+    g = sg.Graph.sbm(16000, 8, 0.2, 0.002, 512, seed=7)
+    for mu in (2, 20):
+        assert_same_as_oracle(g, eps, mu, EXACT)
+        assert_same_as_oracle(g, eps, mu, REF)
+
+
+def test_sbm_pipeline(bitmap):
     g = sg.Graph.sbm(5000, 8, 0.1, 0.001, 64, seed=3)
     for eps in ("0.3", "0.5", "0.7"):
         for mu in (2, 5, 8):
@@ -203,6 +264,39 @@ def test_repeat_runs_identical():
     a = g.run("0.5", 5, EXACT)
     b = g.run("0.5", 5, EXACT)
     assert np.array_equal(a.label, b.label) and np.array_equal(a.role, b.role)
+
+
+def test_degree_prune_leaves_no_stale_cache(bitmap):
+    """A one-shot run skips the edges its eps rules out by degree; those partial counts must
+    never be served later as cached counts."""
+    g = sg.Graph.rmat(12, 16, seed=6)
+    assert_same_as_oracle(g, "0.8", 5, EXACT)          # prunes most hub edges
+    cn, _ = g.common_neighbors()
+    assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
+    assert_same_as_oracle(g, "0.8", 5, REF)
+    cl, vx = g.memberships("0.2", 2, EXACT)
+    ocl, ovx = oracle.memberships(g.offsets(), g.adjacency(), "0.2", 2, EXACT)
+    assert np.array_equal(cl, ocl) and np.array_equal(vx, ovx)
+    assert_same_as_oracle(g, "0.2", 2, EXACT)
+
+
+def prune_boundary_graph(extra):
+    # v has degree 15 (dv + 1 = 16); u has degree 3 (du + 1 = 4) with N(u) = {v, a, b} and
+    # a, b also adjacent to v, so T(u, v) = 2.  At eps = 1/2: du + 1 = eps^2 (dv + 1) sits
+    # exactly on the prune boundary and (T + 2)^2 = eps^2 (du + 1)(dv + 1) = 16: similar.
+    v, u, a, b = 0, 1, 2, 3
+    edges = [(v, u), (v, a), (v, b), (u, a), (u, b)] + [(v, 4 + i) for i in range(12)]
+    edges += [(4 + i, 16 + j) for i in range(12) for j in range(extra)]
+    return sg.Graph.from_edges(16 + extra, edges)
+
+
+@pytest.mark.parametrize("eps", ["0.5", "0.5000001", "0.4999999", "0.25", "1", "1.5", "0"])
+@pytest.mark.parametrize("extra", [0, 3])
+def test_degree_prune_boundary(eps, extra):
+    g = prune_boundary_graph(extra)
+    for mode in (EXACT, REF):
+        for mu in (1, 2, 3):
+            assert_same_as_oracle(g, eps, mu, mode)
 
 
 def test_memberships_match_oracle():
