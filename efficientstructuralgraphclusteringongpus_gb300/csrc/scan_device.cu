@@ -414,7 +414,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     // Task plan.
     PlanParams pp;
     pp.target_probes = 1ull << 22;
-    pp.target_probes_bitmap = 1ull << 23;
+    pp.target_probes_bitmap = 1ull << 25;   // bitmap tasks: 8x, each pays a CTA-wide barrier
     pp.min_slice_edges = 64;
     pp.chunk_max = kChunkMax;
     SCAN_TRY(plan_tasks(d.get(), pp));
@@ -507,7 +507,7 @@ scan_status autotune_similarity(DeviceGraph* d, float* best_ms) {
     for (int trial = 0; trial < 6; ++trial) {
         PlanParams pp = base;
         pp.target_probes = probes[trial % 3];
-        pp.target_probes_bitmap = 2 * pp.target_probes;
+        pp.target_probes_bitmap = 8 * pp.target_probes;
         pp.chunk_max = chunks[trial / 3];
         SCAN_TRY(plan_tasks(d, pp));
         for (uint32_t lw : longs) {
