@@ -56,7 +56,8 @@ struct DeviceGraph {
     uint32_t* lo_adj = nullptr;
     uint32_t* lo_src = nullptr;
     unsigned long long* work = nullptr;
-    unsigned long long* cn_ctr = nullptr;   // last launch_cn: [0] 16-byte list words read, [1] edges counted
+    unsigned long long* cn_ctr = nullptr;
+    uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;
     uint32_t nsmall = 0;
     scan::CnTask* big[scan::kNumBigClasses] = {};

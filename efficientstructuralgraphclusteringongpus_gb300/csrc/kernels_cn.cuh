@@ -339,15 +339,26 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
     return cnt;
 }
 
-__global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap,
+// Next task of a persistent CTA: from the launch's queue counter (dynamic: a CTA that drew
+// short tasks takes more), or blockIdx-strided when queue is null.  Every thread calls it;
+// it holds a CTA barrier.
+__device__ __forceinline__ uint32_t next_task(uint32_t* queue, uint32_t prev, bool first, uint32_t* slot) {
+    if (!queue) return first ? blockIdx.x : prev + gridDim.x;
+    if (threadIdx.x == 0) *slot = atomicAdd(queue, 1u);
+    __syncthreads();
+    return *slot;
+}
+
+__global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap, uint32_t* queue,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
                          CnPrune pr, unsigned long long* __restrict__ ctr) {
     extern __shared__ __align__(16) uint32_t tab[];
-    __shared__ uint32_t next_batch;
+    __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nb = cap / 4;
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
+         t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
         for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
             reinterpret_cast<uint4*>(tab)[i] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
@@ -423,17 +434,18 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
 
 // task.cb carries the pivot's tail size.
 __global__ void __launch_bounds__(kBitmapThreads, 1)
-k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ off,
+k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn,
             uint32_t long_words, CnPrune pr, unsigned long long* __restrict__ ctr) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* bits = smem;                              // kHotBits / 32 words
     uint32_t* tail = smem + kHotBits / 32;              // kTailSlots words
-    __shared__ uint32_t next_batch;
+    __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t i = threadIdx.x; i < kHotBits / 128; i += blockDim.x)
         reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
+         t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
         uint32_t ntb = 8;                                // tail buckets: >= tail size (load <= 1/4),

@@ -422,6 +422,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     // Result and scratch arrays.
     SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
     SCAN_TRY(dalloc(d.get(), &d->cn_ctr, 2));
+    SCAN_TRY(dalloc(d.get(), &d->task_queue, 8));
     uint8_t* rs_mem = nullptr;
     SCAN_TRY(dalloc(d.get(), &rs_mem, run_scratch_bytes(d->n, d->E)));
     run_scratch_bind(&d->rs, rs_mem, d->n, d->E);
@@ -448,6 +449,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u};
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
+    SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
     SCAN_CUDA(cudaEventRecord(d->ev[7], s));
     if (d->nsmall) {
         constexpr int kWpb = 8;
@@ -464,7 +466,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     }
     for (int c = 0; c < kNumBigClasses; ++c) {
         if (d->nbig[c]) {
-            const int threads = c == 0 ? 256 : 512;
+            const int threads = c == 0 ? 128 : 512;   // class 0: many small pivots, measured fastest
             const size_t smem = big_class_slots(c) * sizeof(uint32_t);
             int& per_sm = g_per_sm[d->device][c];
             if (per_sm == 0) {
@@ -472,7 +474,8 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
                 per_sm = std::max(per_sm, 1);
             }
             const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-            k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c), d->off,
+            k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
+                                                            d->task_queue + c, d->off,
                                                             d->adj, d->lo_adj, d->cn, d->long_words, pr,
                                                             d->cn_ctr);
             ++*launches;
@@ -486,7 +489,8 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
             g_attr_bitmap[d->device] = true;
         }
         const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
-        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->off, d->radj, d->lo_adj, d->cn,
+        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->task_queue + 3, d->off, d->radj,
+                                                                  d->lo_adj, d->cn,
                                                                   d->long_words, pr, d->cn_ctr);
         ++*launches;
     }
