@@ -57,7 +57,8 @@ struct DeviceGraph {
     uint32_t* lo_src = nullptr;
     unsigned long long* work = nullptr;
     unsigned long long* cn_ctr = nullptr;
-    uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel   // last launch_cn: [0] 16-byte list words read, [1] edges counted
+    uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel
+    bool has_split = false;                // the plan splits some pivot into chunks   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;
     uint32_t nsmall = 0;
     scan::CnTask* big[scan::kNumBigClasses] = {};
@@ -100,7 +101,11 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 // cn for every edge on d->stream.
 // cn for every edge; with `prune`, edges that the degree prune rules out at that eps are
 // skipped and keep cn = 0 (a one-shot run; the result is not a reusable cache).
-scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune = nullptr);
+// With `fused` (a one-shot run whose plan splits no pivot), the kernels also run the
+// predicate: sim, sd and the run counters must be zeroed before, and launch_cluster is
+// then told so (predicate_done).
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune = nullptr,
+                      const RunScratch* fused = nullptr);
 // Rebuild the similarity tasks for plan parameters pp.
 scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp);
 // Time launch_cn under a few (task size, long-list threshold) settings and keep the fastest;
@@ -117,7 +122,7 @@ struct BatchParams {
 // predicate -> cores -> union-find -> attach -> classify from d->cn into r, on stream s.
 // No host synchronisation.  bp (may be null) gives per-graph parameters.
 scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
-                           uint32_t* launches, const BatchParams* bp = nullptr);
+                           uint32_t* launches, const BatchParams* bp = nullptr, bool predicate_done = false);
 // eps text + mode -> predicate parameters.
 scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode);
 

@@ -112,7 +112,52 @@ struct CnPrune {
     double eps;
     uint64_t p, q;
     uint32_t on;
+    int mode;        // the run's predicate (PredParams::mode), for the fused predicate
 };
+
+// Predicate fused into the counting kernels of a one-shot run whose plan splits no pivot:
+// the count of edge k is final when its lane holds it, so the eps test, the
+// similar-degree counts and the run counters are done there instead of in k_predicate
+// (which would read every edge, its endpoints and both degrees once more).  sim null:
+// counts only.  sim must start zeroed (pruned edges of k_cn_small are not written).
+struct FusedPred {
+    uint8_t* sim;
+    int32_t* sd;
+    RunCounters* ctr;
+};
+
+// Warp-wide (holds a ballot): every lane calls it; lanes with valid set test edge k
+// {u lower, v pivot} with count t.  v is the same for every lane of the call.
+__device__ __forceinline__ void fused_predicate(const FusedPred& fp, const CnPrune& pr, bool valid, uint32_t k,
+                                                uint32_t u, uint32_t v, uint32_t du, uint32_t dv, uint32_t t,
+                                                uint32_t lane, unsigned long long& nsim, unsigned long long& ndis) {
+    bool s = false;
+    if (valid) {
+        const bool r = ref_f64_similar(t, du, dv, pr.eps);
+        const bool x = exact_similar(t, du, dv, pr.p, pr.q);
+        s = pr.mode ? r : x;
+        ndis += (r != x);
+        nsim += s;
+        fp.sim[k] = s;
+        if (s) atomicAdd(&fp.sd[u], 1);
+    }
+    const uint32_t nv = __popc(__ballot_sync(0xFFFFFFFFu, s));
+    if (lane == 0 && nv) atomicAdd(&fp.sd[v], (int32_t)nv);
+}
+
+// End of a fused kernel: the warp's similar-edge and disagreement totals to the counters.
+__device__ __forceinline__ void fused_totals(const FusedPred& fp, uint32_t lane, unsigned long long nsim,
+                                             unsigned long long ndis) {
+    if (!fp.sim) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        nsim += __shfl_xor_sync(0xFFFFFFFFu, nsim, o);
+        ndis += __shfl_xor_sync(0xFFFFFFFFu, ndis, o);
+    }
+    if (lane == 0) {
+        if (nsim) atomicAdd(&fp.ctr->similar_edges, nsim);
+        if (ndis) atomicAdd(&fp.ctr->disagreements, ndis);
+    }
+}
 
 __device__ __forceinline__ bool cn_pruned(uint32_t du, uint32_t dv, const CnPrune& pr) {
     return pr.on && ref_f64_never(du, dv, pr.eps) && exact_never(du, dv, pr.p, pr.q);
@@ -142,11 +187,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
            const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, CnPrune pr,
-           unsigned long long* __restrict__ ctr) {
+           unsigned long long* __restrict__ ctr, FusedPred fp) {
     __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* tab = tabs[wib];
     const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+    unsigned long long nsim = 0, ndis = 0;
     for (uint32_t t = blockIdx.x * kWarpsPerBlock + wib; t < npiv; t += nwarps) {
         const uint32_t v = pivots[t];
         const uint32_t b = off[v], e = off[v + 1];
@@ -157,16 +203,35 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
         __syncwarp();
         const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
         uint32_t words = 0, counted = 0;
-        for (uint32_t k = k0; k < k1; ++k) {
-            const uint32_t u = lo_adj[k];
-            const uint32_t ub = off[u], ue = off[u + 1];
-            if (cn_pruned(ue - ub, e - b, pr)) continue;     // cn[k] stays 0
-            words += (ue - ub + 3u) >> 2;
-            ++counted;
-            uint32_t c = 0;
-            for (uint32_t j = ub + lane; j < ue; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
-            c = __reduce_add_sync(0xFFFFFFFFu, c);
-            if (lane == 0) cn[k] = c;
+        // 32 lower edges at a time: lane i loads edge i's endpoint and list bounds (the
+        // dependent loads of 32 edges overlap), then the warp counts the lists one by one
+        // and lane i keeps edge i's count.
+        for (uint32_t kb = k0; kb < k1; kb += 32) {
+            const uint32_t kk = kb + lane;
+            const bool vk = kk < k1;
+            uint32_t mu_ = 0, mub = 0, mue = 0, mc = 0;
+            if (vk) {
+                mu_ = lo_adj[kk];
+                mub = off[mu_];
+                mue = off[mu_ + 1];
+                if (cn_pruned(mue - mub, e - b, pr)) mue = mub;   // cn stays 0
+            }
+            const uint32_t nk = min(32u, k1 - kb);
+            for (uint32_t i = 0; i < nk; ++i) {
+                const uint32_t ub = __shfl_sync(0xFFFFFFFFu, mub, i), ue = __shfl_sync(0xFFFFFFFFu, mue, i);
+                if (ue == ub) continue;
+                words += (ue - ub + 3u) >> 2;
+                ++counted;
+                uint32_t c = 0;
+                for (uint32_t j = ub + lane; j < ue; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
+                c = __reduce_add_sync(0xFFFFFFFFu, c);
+                if (lane == i) mc = c;
+            }
+            if (vk) cn[kk] = mc;
+            if (fp.sim) {
+                const uint32_t du = vk ? off[mu_ + 1] - off[mu_] : 0u;
+                fused_predicate(fp, pr, vk, kk, mu_, v, du, e - b, mc, lane, nsim, ndis);
+            }
         }
         if (lane == 0 && counted) {
             atomicAdd(&ctr[0], (unsigned long long)words);
@@ -174,6 +239,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
         }
         __syncwarp();
     }
+    fused_totals(fp, lane, nsim, ndis);
 }
 
 // Larger pivots: one CTA per task; a bucketed table of `cap` slots (cap/4 buckets) in
@@ -352,11 +418,12 @@ __device__ __forceinline__ uint32_t next_task(uint32_t* queue, uint32_t prev, bo
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap, uint32_t* queue,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
-                         CnPrune pr, unsigned long long* __restrict__ ctr) {
+                         CnPrune pr, unsigned long long* __restrict__ ctr, FusedPred fp) {
     extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nb = cap / 4;
+    unsigned long long nsim = 0, ndis = 0;
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
@@ -376,13 +443,14 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
             if (kb >= tk.e1) break;
             const uint32_t k = kb + lane;
             const bool valid = k < tk.e1;
-            uint32_t ub = 0, ue = 0;
+            uint32_t ub = 0, ue = 0, u = 0, du = 0;
             bool counted = false;
             if (valid) {
-                const uint32_t u = lo_adj[k];
+                u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
-                if (cn_pruned(ue - ub, ve - vb, pr)) ue = ub;
+                du = ue - ub;
+                if (cn_pruned(du, ve - vb, pr)) ue = ub;
                 counted = ue > ub && tk.cb == vb;               // once per edge: in its first chunk
                 if (tk.chunked && ue > ub) {
                     if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
@@ -404,9 +472,11 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 if (!tk.chunked) cn[k] = cnt;
                 else if (cnt) atomicAdd(&cn[k], cnt);           // cn was zeroed before the launch
             }
+            if (fp.sim) fused_predicate(fp, pr, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
         }
         __syncthreads();
     }
+    fused_totals(fp, lane, nsim, ndis);
 }
 
 // Bitmap path: one CTA of kBitmapThreads per task (pivot, edge slice), one CTA per SM.
@@ -436,12 +506,13 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
 __global__ void __launch_bounds__(kBitmapThreads, 1)
 k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn,
-            uint32_t long_words, CnPrune pr, unsigned long long* __restrict__ ctr) {
+            uint32_t long_words, CnPrune pr, unsigned long long* __restrict__ ctr, FusedPred fp) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* bits = smem;                              // kHotBits / 32 words
     uint32_t* tail = smem + kHotBits / 32;              // kTailSlots words
     __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
+    unsigned long long nsim = 0, ndis = 0;
     for (uint32_t i = threadIdx.x; i < kHotBits / 128; i += blockDim.x)
         reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
@@ -468,12 +539,13 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
             if (kb >= tk.e1) break;
             const uint32_t k = kb + lane;
             const bool valid = k < tk.e1;
-            uint32_t ub = 0, ue = 0;
+            uint32_t ub = 0, ue = 0, u = 0, du = 0;
             if (valid) {
-                const uint32_t u = lo_adj[k];
+                u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
-                if (cn_pruned(ue - ub, ve - vb, pr)) ue = ub;
+                du = ue - ub;
+                if (cn_pruned(du, ve - vb, pr)) ue = ub;
             }
             const uint32_t tlo = (pr.on && ue > ub) ? min_similar_count(ue - ub, ve - vb, pr) : 0u;
             uint32_t words = 0;
@@ -488,6 +560,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
+            if (fp.sim) fused_predicate(fp, pr, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
         }
         __syncthreads();
         for (uint32_t j = vb + threadIdx.x; j < ve; j += blockDim.x) {   // clear this pivot's bits
@@ -496,10 +569,12 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
         }
         __syncthreads();
     }
+    fused_totals(fp, lane, nsim, ndis);
 }
 
 // Task planner.  Pass 1 (outputs null) counts tasks per class; pass 2 writes them.
-// counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks.
+// counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks,
+// counts[5] (pass 1 only) pivots split into chunks.
 // tail (may be null: bitmap path off) holds each vertex's count of non-hot neighbours.
 // (PlanParams: device_graph.h.)
 
@@ -538,6 +613,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                 const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
                 nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
                 ntask = nch * nsl;
+                if (nch > 1 && small_out == nullptr) atomicAdd(&counts[2 + kNumBigClasses], 1u);   // split pivots
             }
         }
     }

@@ -253,10 +253,10 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
     cudaStream_t s = d->stream;
     uint32_t* counts = d->dflags + 1;
     const unsigned pg = (unsigned)((d->n + 255) / 256);
-    SCAN_CUDA(cudaMemsetAsync(counts, 0, (2 + kNumBigClasses) * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, (3 + kNumBigClasses) * sizeof(uint32_t), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
                               nullptr, nullptr);
-    uint32_t hc[2 + kNumBigClasses];
+    uint32_t hc[3 + kNumBigClasses];
     SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
     // task arrays: reuse the current ones when large enough
@@ -273,6 +273,7 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
         SCAN_TRY(ensure(&d->big[c], &d->cap_big[c], d->nbig[c]));
     }
     d->nbmp = hc[1 + kNumBigClasses];
+    d->has_split = hc[2 + kNumBigClasses] > 0;
     SCAN_TRY(ensure(&d->bmp, &d->cap_bmp, d->nbmp));
     SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
@@ -443,10 +444,12 @@ static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class 
                                                 // so capturing launch_cn into a graph queries nothing)
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
-scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune) {
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune, const RunScratch* fused) {
     cudaStream_t s = d->stream;
-    CnPrune pr{0.0, 0, 1, 0u};
-    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u};
+    CnPrune pr{0.0, 0, 1, 0u, 0};
+    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u, prune->mode};
+    FusedPred fp{nullptr, nullptr, nullptr};
+    if (fused && prune && !d->has_split) fp = FusedPred{fused->sim, fused->sd, fused->ctr};
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
     SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
@@ -454,7 +457,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     if (d->nsmall) {
         constexpr int kWpb = 8;
         k_cn_small<kWpb><<<grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16), kWpb * 32, 0, s>>>(
-            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, pr, d->cn_ctr);
+            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, pr, d->cn_ctr, fp);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
@@ -477,7 +480,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
             k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
                                                             d->task_queue + c, d->off,
                                                             d->adj, d->lo_adj, d->cn, d->long_words, pr,
-                                                            d->cn_ctr);
+                                                            d->cn_ctr, fp);
             ++*launches;
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
@@ -491,7 +494,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
         const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
         k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->task_queue + 3, d->off, d->radj,
                                                                   d->lo_adj, d->cn,
-                                                                  d->long_words, pr, d->cn_ctr);
+                                                                  d->long_words, pr, d->cn_ctr, fp);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
@@ -545,17 +548,22 @@ static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
 // predicate -> cores -> union-find -> attach -> classify, on cached cn.  Queued on s with
 // no host synchronisation.
 scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
-                           uint32_t* launches, const BatchParams* bp) {
+                           uint32_t* launches, const BatchParams* bp, bool predicate_done) {
     const uint64_t E = d->E;
     const uint32_t n = d->n;
     const int sms = d->num_sms, T = 256;
     const int ge = grid_for_n(sms, E, T), gn = grid_for_n(sms, n, T);
-    SCAN_CUDA(cudaMemsetAsync(r.sd, 0, n * sizeof(int32_t), s));
-    SCAN_CUDA(cudaMemsetAsync(r.ctr, 0, sizeof(RunCounters), s));
+    if (!predicate_done) {
+        SCAN_CUDA(cudaMemsetAsync(r.sd, 0, n * sizeof(int32_t), s));
+        SCAN_CUDA(cudaMemsetAsync(r.ctr, 0, sizeof(RunCounters), s));
+    }
     SCAN_CUDA(cudaMemsetAsync(r.jump_flags, 0, kMaxJumpRounds * sizeof(uint32_t), s));
     const uint32_t* vgid = bp ? bp->vgid : nullptr;
-    k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr, r.sim, r.sd,
-                                 r.ctr);
+    if (!predicate_done) {
+        k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr, r.sim,
+                                     r.sd, r.ctr);
+        ++*launches;
+    }
     k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
     k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
     const uint32_t rounds = jump_rounds(n);
@@ -564,7 +572,7 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     k_label<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.lab);
     k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax);
     k_finalize<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.bmax, r.nmin, r.nmax, r.label, r.role, r.ctr);
-    *launches += 7 + rounds;
+    *launches += 6 + rounds;
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }
@@ -605,12 +613,20 @@ static scan_status run_resident(DeviceGraph* d, const PredParams& pp, int mu, bo
     SCAN_CUDA(cudaEventRecord(d->ev[3], s));
     d->cn_valid_before = d->cn_valid;
     const bool count = !(reuse_cn && d->cn_valid);
+    // With no split pivot, the counting kernels also run the predicate (each count is final
+    // in the lane that computes it).
+    const bool fused = count && !d->has_split;
     if (count) {
         d->cn_valid = false;
-        SCAN_TRY(launch_cn(d, &launches, &pp));
+        if (fused) {
+            SCAN_CUDA(cudaMemsetAsync(d->rs.sim, 0, d->E, s));
+            SCAN_CUDA(cudaMemsetAsync(d->rs.sd, 0, d->n * sizeof(int32_t), s));
+            SCAN_CUDA(cudaMemsetAsync(d->rs.ctr, 0, sizeof(RunCounters), s));
+        }
+        SCAN_TRY(launch_cn(d, &launches, &pp, fused ? &d->rs : nullptr));
     }
     SCAN_CUDA(cudaEventRecord(d->ev[4], s));
-    SCAN_TRY(launch_cluster(d, d->rs, s, pp, mu, &launches));
+    SCAN_TRY(launch_cluster(d, d->rs, s, pp, mu, &launches, nullptr, fused));
     SCAN_CUDA(cudaEventRecord(d->ev[5], s));
     RunCounters hc;
     uint32_t last_round = 0;
