@@ -10,6 +10,12 @@ cores, union-find, attach, hub/outlier) over the graph.
             CSR buffers to host labels: H2D, orientation, SCAN, D2H and device allocation
   roofline  the common-neighbour stage, HBM bound
   cpu_baseline  the oracle (a plain OpenMP merge-intersection SCAN) on a bounded edge sample
+  sweep     eps in {0.2, 0.4, 0.6, 0.8} x mu in {2, 5, 10} on the same resident graph
+  serving / batch   the serving loop and the batched small graphs (their own configs)
+
+  --chung-lu  instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices,
+              ~1B undirected edges, max degree 2M, eps 0.4, mu 5), resident and streamed
+              under a 24 GB device cap (several minutes; not part of the default run)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has
@@ -59,6 +65,14 @@ def parse():
     ap.add_argument("--batch-only", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--batch-max-n", type=int, default=10000)
+    ap.add_argument("--no-sweep", action="store_true", help="skip the eps x mu sweep on the bench graph")
+    ap.add_argument("--chung-lu", action="store_true",
+                    help="instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices, ~1B edges, "
+                         "max degree 2M, eps 0.4, mu 5), resident and streamed under a 24 GB device cap")
+    ap.add_argument("--cl-vertices", type=int, default=50_000_000)
+    ap.add_argument("--cl-edges", type=int, default=1_000_000_000)
+    ap.add_argument("--cl-cap", type=int, default=2_000_000)
+    ap.add_argument("--cl-budget-gb", type=float, default=24.0)
     ap.add_argument("--reference-kernels", action="store_true",
                     help="with --impl reference: time the reference's own GPU kernels (its cubin) instead")
     return ap.parse_args()
@@ -358,6 +372,64 @@ def reference_arm(args) -> None:
     }))
 
 
+def sweep_bench(g, args, mode, device: int) -> list:
+    """The eps x mu sweep of the scale-22 config: one warm and two timed one-shot runs each;
+    device ms (similarity + cluster stages) and edges/s."""
+    out = []
+    for eps in ("0.2", "0.4", "0.6", "0.8"):
+        for mu in (2, 5, 10):
+            g.run(eps, mu, mode, device=device)
+            ms = []
+            for _ in range(2):
+                st = g.run(eps, mu, mode, device=device).stats
+                ms.append(st["ms_similarity"] + st["ms_cluster"])
+            t = float(np.mean(ms))
+            out.append({"eps": eps, "mu": mu, "ms": t, "edges_per_s": g.num_edges / (t / 1e3),
+                        "cores": st["num_cores"], "clusters": st["num_clusters"],
+                        "similar_edges": st["num_similar_edges"]})
+    return out
+
+
+def chung_lu_bench(args, device: int) -> dict:
+    """Skewed hub-heavy config: the graph resident in HBM, then streamed (adjacency in pinned
+    host memory read over the host link, the rest under a device cap); labels must agree."""
+    import efficientstructuralgraphclusteringongpus_gb300 as sg
+
+    mode = sg.PRED_REF_F64 if args.predicate == "ref-f64" else sg.PRED_EXACT
+    t = time.perf_counter()
+    g = sg.Graph.chung_lu(args.cl_vertices, 2.1, args.cl_edges, args.cl_cap, seed=args.seed)
+    gen_s = time.perf_counter() - t
+    eps, mu = "0.4", 5
+    out = {"workload": f"chung-lu-{args.cl_vertices}v-{args.cl_edges}e-cap{args.cl_cap}", "n": g.n,
+           "undirected_edges": g.num_edges, "max_degree": g.max_degree, "eps": eps, "mu": mu,
+           "predicate": args.predicate, "generate_s": gen_s}
+
+    def timed(tag):
+        g.run(eps, mu, mode, device=device)
+        runs = [g.run(eps, mu, mode, device=device) for _ in range(max(args.steps, 1))]
+        ms = [r.stats["ms_similarity"] + r.stats["ms_cluster"] for r in runs]
+        st = runs[-1].stats
+        out[tag] = {"ms_per_step": float(np.mean(ms)), "edges_per_s": g.num_edges / (float(np.mean(ms)) / 1e3),
+                    "ms_similarity": st["ms_similarity"], "cores": st["num_cores"], "clusters": st["num_clusters"],
+                    "similar_edges": st["num_similar_edges"], "device_bytes": g.device_bytes}
+        return runs[-1].label
+
+    t = time.perf_counter()
+    g.upload(device)
+    out["upload_s"] = time.perf_counter() - t
+    lab = timed("resident")
+    g.release_device()
+    t = time.perf_counter()
+    used = g.upload_streamed(device, int(args.cl_budget_gb * (1 << 30)))
+    out["streamed_upload_s"] = time.perf_counter() - t
+    lab2 = timed("streamed")
+    out["streamed"]["budget_bytes"] = int(args.cl_budget_gb * (1 << 30))
+    out["streamed"]["device_bytes_used"] = used
+    out["streamed_labels_equal_resident"] = bool(np.array_equal(lab, lab2))
+    g.release_device()
+    return out
+
+
 def reference_kernels_arm(args) -> None:
     """The reference's own GPU kernels (GPUSCAN++/GPUScan.cu compiled unmodified into a cubin)
     on this GPU, replayed by the oracle's harness in GPUScan()'s launch order
@@ -419,6 +491,11 @@ def main():
     torch.cuda.set_device(local)
     dist = Dist(world, "nccl")
     mode = sg.PRED_REF_F64 if args.predicate == "ref-f64" else sg.PRED_EXACT
+    if args.chung_lu:
+        if rank == 0:
+            print(json.dumps({"chung_lu": chung_lu_bench(args, local)}))
+        dist.close()
+        return
     if args.serving_only or args.batch_only:
         if rank == 0:
             out = {"serving": serving_bench(args, local)} if args.serving_only else {"batch": batch_bench(args, local)}
@@ -501,6 +578,7 @@ def main():
         cpu = None
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(g, args.eps, args.mu, mode, args.cpu_seconds)
+        sweep = None if args.no_sweep else sweep_bench(g, args, mode, local)
         serving = None if args.no_serving else serving_bench(args, local)
         batch = None if args.no_batch else batch_bench(args, local)
         result = {
@@ -517,6 +595,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
+            "sweep": sweep,
             "serving": serving,
             "batch": batch,
             "stages_ms": {"similarity": float(np.mean(sim_ms)),
