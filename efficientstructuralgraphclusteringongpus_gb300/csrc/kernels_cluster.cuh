@@ -130,6 +130,43 @@ __global__ void k_jump_round(uint32_t n, int32_t* parent, uint32_t* flags, uint3
     if (__any_sync(0xFFFFFFFFu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[round], 1u);
 }
 
+// The same rounds in one CTA, for graphs of up to kJumpBlockMax vertices: a block barrier
+// separates the rounds, so one launch replaces the chain of k_jump_round launches (the
+// launch count matters for the many small queries of the serving loop).  flags follow the
+// chain's convention: flags[i] != 0 when round i moved a pointer, so flags[rounds - 1] == 0
+// means converged.
+constexpr uint32_t kJumpBlockMax = 1u << 16;
+
+__global__ void __launch_bounds__(1024) k_jump_block(uint32_t n, int32_t* parent, uint32_t* flags, uint32_t rounds) {
+    volatile int32_t* vp = parent;
+    for (uint32_t round = 0; round < rounds; ++round) {
+        int ch = 0;
+        for (uint32_t v = threadIdx.x; v < n; v += blockDim.x) {
+            const int32_t p = vp[v];
+            if (p < 0) continue;
+            const int32_t g = vp[p];
+            if (g != p) {
+                vp[v] = g;
+                ch = 1;
+            }
+        }
+        ch = __syncthreads_or(ch);
+        if (threadIdx.x == 0) flags[round] = ch ? 1u : 0u;
+        if (!ch) break;
+    }
+}
+
+// Zeroes a run's similar-degree counts (sd may be null: already done), counters and
+// round flags in one launch.
+__global__ void k_cluster_reset(uint32_t n, int32_t* sd, RunCounters* ctr, uint32_t* flags, uint32_t nflags) {
+    const uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    if (sd)
+        for (uint64_t v = i0; v < n; v += stride) sd[v] = 0;
+    if (i0 < nflags) flags[i0] = 0;
+    if (ctr && i0 == 0) *ctr = RunCounters{};
+}
+
 // Border attachment: a non-core similar to a core joins that core's cluster.  The
 // reference keeps the last write among several clusters (GPUSCAN++/GPUScan.cu:716,722);
 // here the smallest cluster id wins, and bmin != bmax marks a multi-cluster border.

@@ -200,6 +200,8 @@ size_t run_scratch_bytes(uint32_t n, uint64_t E) {
            align256(4 * kMaxJumpRounds);
 }
 
+// The order is relied on: role follows label, and the round flags follow the counters
+// (each padded to 256 bytes), so the serving loop copies each pair back in one transfer.
 void run_scratch_bind(RunScratch* r, void* base, uint32_t n, uint64_t E) {
     char* p = static_cast<char*>(base);
     auto take = [&](size_t bytes) { char* q = p; p += align256(bytes); return q; };
@@ -553,11 +555,9 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     const uint32_t n = d->n;
     const int sms = d->num_sms, T = 256;
     const int ge = grid_for_n(sms, E, T), gn = grid_for_n(sms, n, T);
-    if (!predicate_done) {
-        SCAN_CUDA(cudaMemsetAsync(r.sd, 0, n * sizeof(int32_t), s));
-        SCAN_CUDA(cudaMemsetAsync(r.ctr, 0, sizeof(RunCounters), s));
-    }
-    SCAN_CUDA(cudaMemsetAsync(r.jump_flags, 0, kMaxJumpRounds * sizeof(uint32_t), s));
+    k_cluster_reset<<<gn, T, 0, s>>>(n, predicate_done ? nullptr : r.sd, predicate_done ? nullptr : r.ctr,
+                                     r.jump_flags, kMaxJumpRounds);
+    ++*launches;
     const uint32_t* vgid = bp ? bp->vgid : nullptr;
     if (!predicate_done) {
         k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr, r.sim,
@@ -567,12 +567,18 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
     k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
     const uint32_t rounds = jump_rounds(n);
-    for (uint32_t i = 0; i < rounds; ++i) k_jump_round<<<gn, T, 0, s>>>(n, r.parent, r.jump_flags, i);
+    if (n <= kJumpBlockMax) {
+        k_jump_block<<<1, 1024, 0, s>>>(n, r.parent, r.jump_flags, rounds);
+        ++*launches;
+    } else {
+        for (uint32_t i = 0; i < rounds; ++i) k_jump_round<<<gn, T, 0, s>>>(n, r.parent, r.jump_flags, i);
+        *launches += rounds;
+    }
     k_attach<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.bmin, r.bmax);
     k_label<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.lab);
     k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax);
     k_finalize<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.bmax, r.nmin, r.nmax, r.label, r.role, r.ctr);
-    *launches += 6 + rounds;
+    *launches += 6;
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }

@@ -106,10 +106,12 @@ struct Slot {
     cudaEvent_t ev_start = nullptr, ev_end = nullptr;
     Query* q = nullptr;
     uint64_t arena_off = 0, arena_bytes = 0;
-    int32_t* h_label = nullptr;      // pinned staging, capacity n_cap
-    uint8_t* h_role = nullptr;
-    RunCounters* h_ctr = nullptr;
-    uint32_t* h_flag = nullptr;
+    // Pinned staging.  The run scratch keeps label[n] and role[n] adjacent (label padded
+    // to 256 bytes), and the counters next to the round flags, so each pair comes back in
+    // one copy: h_res holds label then role at res_role_offset(n); h_tail the counters
+    // then the flags at kTailFlags.
+    char* h_res = nullptr;           // capacity for n_cap vertices
+    char* h_tail = nullptr;
     uint32_t n_cap = 0;
     std::atomic<bool> gpu_done{false};
     bool launching = false;          // assigned to q, CUDA work being queued (outside the lock)
@@ -151,6 +153,12 @@ void CUDART_CB on_slot_done(void* arg) {
     delete pair;
 }
 
+size_t pad256(size_t x) { return (x + 255) & ~size_t(255); }
+size_t res_role_offset(uint32_t n) { return pad256(4ull * n); }
+size_t res_bytes(uint32_t n) { return res_role_offset(n) + n; }
+const size_t kTailFlags = pad256(sizeof(RunCounters));
+const size_t kTailBytes = kTailFlags + 4 * kMaxJumpRounds;
+
 uint32_t jump_flag_index(uint32_t n) {
     uint32_t r = 2;
     while ((1ull << (r - 2)) < (uint64_t)n + 1 && r < (uint32_t)kMaxJumpRounds) ++r;
@@ -167,10 +175,8 @@ uint32_t launch_query(scan_server* s, Slot& sl, Query* q) {
     cudaStream_t st = sl.stream;
     cudaEventRecord(sl.ev_start, st);
     scan_status rc = launch_cluster(g, r, st, q->pp, q->mu, &launches);
-    cudaMemcpyAsync(sl.h_label, r.label, g->n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(sl.h_role, r.role, g->n, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(sl.h_ctr, r.ctr, sizeof(RunCounters), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(sl.h_flag, r.jump_flags + jump_flag_index(g->n), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(sl.h_res, r.label, res_bytes(g->n), cudaMemcpyDeviceToHost, st);       // label, role
+    cudaMemcpyAsync(sl.h_tail, r.ctr, kTailBytes, cudaMemcpyDeviceToHost, st);            // counters, flags
     cudaEventRecord(sl.ev_end, st);
     cudaError_t err = cudaLaunchHostFunc(st, on_slot_done, new std::pair<scan_server*, Slot*>(s, &sl));
     if (rc != SCAN_OK || err != cudaSuccess) {
@@ -219,14 +225,16 @@ void scheduler(scan_server* s) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, sl->ev_start, sl->ev_end);
             q->device_ms = ms;
-            q->counters = *sl->h_ctr;
-            if (q->status == SCAN_OK && (q->counters.error_flags || *sl->h_flag)) {
+            std::memcpy(&q->counters, sl->h_tail, sizeof(RunCounters));
+            uint32_t last_flag = 0;
+            std::memcpy(&last_flag, sl->h_tail + kTailFlags + 4 * jump_flag_index(g->n), sizeof(uint32_t));
+            if (q->status == SCAN_OK && (q->counters.error_flags || last_flag)) {
                 q->status = SCAN_ERR_DEVICE;
                 q->error = "union-find did not finish within its limits";
             }
             if (q->status == SCAN_OK) {
-                std::memcpy(q->out_label, sl->h_label, g->n * sizeof(int32_t));
-                if (q->out_role) std::memcpy(q->out_role, sl->h_role, g->n);
+                std::memcpy(q->out_label, sl->h_res, g->n * sizeof(int32_t));
+                if (q->out_role) std::memcpy(q->out_role, sl->h_res + res_role_offset(g->n), g->n);
             }
         }
         {
@@ -315,8 +323,7 @@ scan_status scan_server_create(int device, uint64_t memory_budget_bytes, uint32_
     for (Slot& sl : s->slots) {
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreate(&sl.ev_start) != cudaSuccess || cudaEventCreate(&sl.ev_end) != cudaSuccess ||
-            cudaHostAlloc(&sl.h_ctr, sizeof(RunCounters), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&sl.h_flag, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+            cudaHostAlloc(&sl.h_tail, kTailBytes, cudaHostAllocDefault) != cudaSuccess) {
             scan_server_destroy(s.release());
             return fail(SCAN_ERR_CUDA, "cannot create the server's streams");
         }
@@ -357,13 +364,10 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
         lock.unlock();
         for (Slot& sl : s->slots) {
             if (sl.n_cap >= d->n) continue;
-            if (sl.h_label) cudaFreeHost(sl.h_label);
-            if (sl.h_role) cudaFreeHost(sl.h_role);
-            sl.h_label = nullptr;
-            sl.h_role = nullptr;
+            if (sl.h_res) cudaFreeHost(sl.h_res);
+            sl.h_res = nullptr;
             sl.n_cap = 0;
-            if (cudaHostAlloc(&sl.h_label, d->n * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess ||
-                cudaHostAlloc(&sl.h_role, d->n, cudaHostAllocDefault) != cudaSuccess) {
+            if (cudaHostAlloc(&sl.h_res, res_bytes(d->n), cudaHostAllocDefault) != cudaSuccess) {
                 grow_status = fail(SCAN_ERR_OUT_OF_MEMORY, "cannot allocate pinned result staging");
                 break;
             }
@@ -541,10 +545,8 @@ void scan_server_destroy(scan_server* s) {
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.ev_start) cudaEventDestroy(sl.ev_start);
         if (sl.ev_end) cudaEventDestroy(sl.ev_end);
-        if (sl.h_label) cudaFreeHost(sl.h_label);
-        if (sl.h_role) cudaFreeHost(sl.h_role);
-        if (sl.h_ctr) cudaFreeHost(sl.h_ctr);
-        if (sl.h_flag) cudaFreeHost(sl.h_flag);
+        if (sl.h_res) cudaFreeHost(sl.h_res);
+        if (sl.h_tail) cudaFreeHost(sl.h_tail);
     }
     for (DeviceGraph* d : s->graphs) device_graph_free(d);
     if (s->arena_base) cudaFree(s->arena_base);
