@@ -36,6 +36,8 @@ struct RunCounters {
     unsigned long long cores, clusters, hubs, outliers, borders;
     unsigned long long similar_edges, disagreements, multi_borders;
     uint32_t error_flags;
+    uint32_t any_core;      // set by k_core_init: the edge passes after it return at once when 0
+    uint32_t any_member;    // set by k_label: the hub test's edge pass returns at once when 0
     uint32_t pad;
 };
 

@@ -57,15 +57,20 @@ __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, con
 // runs pass vgid[] and per-graph gmu[].
 __global__ void k_core_init(uint32_t n, const int32_t* __restrict__ sd, int mu, const uint32_t* __restrict__ vgid,
                             const int32_t* __restrict__ gmu, int32_t* __restrict__ parent, int32_t* __restrict__ bmin,
-                            int32_t* __restrict__ bmax, int32_t* __restrict__ nmin, int32_t* __restrict__ nmax) {
+                            int32_t* __restrict__ bmax, int32_t* __restrict__ nmin, int32_t* __restrict__ nmax,
+                            RunCounters* __restrict__ ctr) {
+    bool core = false;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
         const int m = vgid ? gmu[vgid[v]] : mu;
-        parent[v] = sd[v] >= m ? (int32_t)v : -1;
+        const bool c = sd[v] >= m;
+        core |= c;
+        parent[v] = c ? (int32_t)v : -1;
         bmin[v] = 0x7FFFFFFF;
         bmax[v] = -1;
         nmin[v] = 0x7FFFFFFF;
         nmax[v] = -1;
     }
+    if (__any_sync(0xFFFFFFFFu, core) && (threadIdx.x & 31) == 0) atomicOr(&ctr->any_core, 1u);
 }
 
 // Root of x with path halving.  parent[y] < y for every non-root y, so every write keeps
@@ -98,6 +103,7 @@ __device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b) 
 
 __global__ void k_union(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
                         const uint8_t* __restrict__ sim, int32_t* parent, RunCounters* ctr) {
+    if (!*(volatile uint32_t*)&ctr->any_core) return;   // no core: nothing to join
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
         if (!sim[e]) continue;
         const int32_t u = (int32_t)lo_adj[e], v = (int32_t)lo_src[e];
@@ -172,7 +178,8 @@ __global__ void k_cluster_reset(uint32_t n, int32_t* sd, RunCounters* ctr, uint3
 // here the smallest cluster id wins, and bmin != bmax marks a multi-cluster border.
 __global__ void k_attach(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
                          const uint8_t* __restrict__ sim, const int32_t* __restrict__ parent,
-                         int32_t* __restrict__ bmin, int32_t* __restrict__ bmax) {
+                         int32_t* __restrict__ bmin, int32_t* __restrict__ bmax, const RunCounters* ctr) {
+    if (!*(const volatile uint32_t*)&ctr->any_core) return;   // no core: no border
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
         if (!sim[e]) continue;
         const uint32_t u = lo_adj[e], v = lo_src[e];
@@ -184,11 +191,15 @@ __global__ void k_attach(uint64_t E, const uint32_t* __restrict__ lo_adj, const 
 
 // Label after attachment: cluster id for cores and borders, -2 for the rest.
 __global__ void k_label(uint32_t n, const int32_t* __restrict__ parent, const int32_t* __restrict__ bmin,
-                        int32_t* __restrict__ lab) {
+                        int32_t* __restrict__ lab, RunCounters* __restrict__ ctr) {
+    bool member = false;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
         const int32_t p = parent[v];
-        lab[v] = p >= 0 ? p : (bmin[v] != 0x7FFFFFFF ? bmin[v] : -2);
+        const int32_t l = p >= 0 ? p : (bmin[v] != 0x7FFFFFFF ? bmin[v] : -2);
+        lab[v] = l;
+        member |= l >= 0;
     }
+    if (__any_sync(0xFFFFFFFFu, member) && (threadIdx.x & 31) == 0) atomicOr(&ctr->any_member, 1u);
 }
 
 // Hub test inputs: for each unlabelled vertex, the smallest and largest label among its
@@ -196,7 +207,8 @@ __global__ void k_label(uint32_t n, const int32_t* __restrict__ parent, const in
 // second neighbour label different from the first).
 __global__ void k_neighbour_labels(uint64_t E, const uint32_t* __restrict__ lo_adj,
                                    const uint32_t* __restrict__ lo_src, const int32_t* __restrict__ lab,
-                                   int32_t* __restrict__ nmin, int32_t* __restrict__ nmax) {
+                                   int32_t* __restrict__ nmin, int32_t* __restrict__ nmax, const RunCounters* ctr) {
+    if (!*(const volatile uint32_t*)&ctr->any_member) return;   // no cluster: every other vertex is an outlier
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t u = lo_adj[e], v = lo_src[e];
         const int32_t lu = lab[u], lv = lab[v];

@@ -564,7 +564,8 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
                                      r.sd, r.ctr);
         ++*launches;
     }
-    k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax);
+    k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax,
+                                 r.ctr);
     k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
     const uint32_t rounds = jump_rounds(n);
     if (n <= kJumpBlockMax) {
@@ -574,9 +575,9 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
         for (uint32_t i = 0; i < rounds; ++i) k_jump_round<<<gn, T, 0, s>>>(n, r.parent, r.jump_flags, i);
         *launches += rounds;
     }
-    k_attach<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.bmin, r.bmax);
-    k_label<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.lab);
-    k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax);
+    k_attach<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.bmin, r.bmax, r.ctr);
+    k_label<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.lab, r.ctr);
+    k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax, r.ctr);
     k_finalize<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.bmax, r.nmin, r.nmax, r.label, r.role, r.ctr);
     *launches += 6;
     SCAN_CUDA(cudaGetLastError());

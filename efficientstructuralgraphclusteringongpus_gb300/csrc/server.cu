@@ -115,6 +115,7 @@ struct Slot {
     uint32_t n_cap = 0;
     std::atomic<bool> gpu_done{false};
     bool launching = false;          // assigned to q, CUDA work being queued (outside the lock)
+    bool finishing = false;          // results being copied out (outside the lock)
 };
 
 }  // namespace
@@ -131,7 +132,13 @@ struct scan_server {
     std::mutex mu;
     std::condition_variable cv_work;   // scheduler: new query or a slot finished
     std::condition_variable cv_done;   // waiters: a query finished
-    std::thread worker;
+    std::thread worker;                // the scheduler
+    // Workers queue each admitted query's CUDA work and copy finished results out, several
+    // at a time: one thread issuing a dozen CUDA calls per query capped the served rate.
+    std::vector<std::thread> workers;
+    std::deque<std::pair<bool, Slot*>> jobs;   // (launch, slot): launch, or copy out and free
+    std::condition_variable cv_jobs;
+    bool stop_workers = false;
     bool stop = false;
     bool mem_blocked = false;          // the queue head waits for arena space to be returned
     bool pause_admission = false;      // a graph is being added
@@ -187,115 +194,135 @@ uint32_t launch_query(scan_server* s, Slot& sl, Query* q) {
     return launches;
 }
 
-bool slot_finished(const Slot& sl) { return sl.q && !sl.launching && sl.gpu_done.load(); }
+bool slot_finished(const Slot& sl) { return sl.q && !sl.launching && !sl.finishing && sl.gpu_done.load(); }
 
-// The scheduler.  Under the lock it only does bookkeeping (which slots finished, which
-// queries to admit, arena blocks); result copies and every CUDA call happen with the lock
-// released, so a device-wide synchronisation elsewhere in the process (cudaMalloc/cudaFree
+// Copy a finished slot's results to the caller's buffers (lock not held).
+void copy_out(Slot* sl) {
+    Query* q = sl->q;
+    DeviceGraph* g = q->graph;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, sl->ev_start, sl->ev_end);
+    q->device_ms = ms;
+    std::memcpy(&q->counters, sl->h_tail, sizeof(RunCounters));
+    uint32_t last_flag = 0;
+    std::memcpy(&last_flag, sl->h_tail + kTailFlags + 4 * jump_flag_index(g->n), sizeof(uint32_t));
+    if (q->status == SCAN_OK && (q->counters.error_flags || last_flag)) {
+        q->status = SCAN_ERR_DEVICE;
+        q->error = "union-find did not finish within its limits";
+    }
+    if (q->status == SCAN_OK) {
+        std::memcpy(q->out_label, sl->h_res, g->n * sizeof(int32_t));
+        if (q->out_role) std::memcpy(q->out_role, sl->h_res + res_role_offset(g->n), g->n);
+    }
+}
+
+// A worker: launches admitted queries and retires finished ones.  CUDA calls and result
+// copies happen with the lock released; the bookkeeping that follows takes it briefly.
+void worker_loop(scan_server* s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        std::pair<bool, Slot*> job;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_jobs.wait(lock, [&] { return !s->jobs.empty() || s->stop_workers; });
+            if (s->jobs.empty()) return;
+            job = s->jobs.front();
+            s->jobs.pop_front();
+        }
+        Slot* sl = job.second;
+        if (job.first) {
+            const uint32_t launches = launch_query(s, *sl, sl->q);
+            std::lock_guard<std::mutex> lock(s->mu);
+            sl->launching = false;
+            s->totals.kernel_launches += launches;
+        } else {
+            copy_out(sl);
+            std::lock_guard<std::mutex> lock(s->mu);
+            Query* q = sl->q;
+            s->arena.release(sl->arena_off, sl->arena_bytes);
+            s->mem_blocked = false;
+            sl->q = nullptr;
+            sl->finishing = false;
+            q->finished = Clock::now();
+            q->done = true;
+            ++s->totals.completed;
+            if (q->status != SCAN_OK) ++s->totals.failed;
+        }
+        s->cv_work.notify_one();
+        s->cv_done.notify_all();
+    }
+}
+
+// The scheduler.  It only does bookkeeping under the lock: which slots finished (handed to
+// the workers to copy out and free), which queries to admit (arena blocks, slots; handed
+// to the workers to launch).  No thread calls into CUDA or copies results while holding
+// the lock, so a device-wide synchronisation elsewhere in the process (cudaMalloc/cudaFree
 // by another thread) can always drain the host callbacks it waits for.
 void scheduler(scan_server* s) {
     cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lock(s->mu);
     for (;;) {
-        std::vector<Slot*> finished;
-        std::vector<Slot*> to_launch;
-        {
-            std::unique_lock<std::mutex> lock(s->mu);
-            s->cv_work.wait(lock, [&] {
-                bool any_busy = false;
-                for (Slot& sl : s->slots) {
-                    if (slot_finished(sl)) return true;
-                    any_busy |= sl.q != nullptr;
-                }
-                if (s->stop && !any_busy && s->pending.empty()) return true;
-                if (s->pending.empty() || s->mem_blocked || s->pause_admission) return false;
-                for (Slot& sl : s->slots)
-                    if (!sl.q) return true;
-                return false;
-            });
-            for (Slot& sl : s->slots)
-                if (slot_finished(sl)) finished.push_back(&sl);
+        s->cv_work.wait(lock, [&] {
             bool any_busy = false;
-            for (Slot& sl : s->slots) any_busy |= sl.q != nullptr;
-            if (s->stop && !any_busy && s->pending.empty()) return;
-        }
-        // results out of the pinned staging (no lock; these slots are not touched elsewhere)
-        for (Slot* sl : finished) {
-            Query* q = sl->q;
+            for (Slot& sl : s->slots) {
+                if (slot_finished(sl)) return true;
+                any_busy |= sl.q != nullptr;
+            }
+            if (s->stop && !any_busy && s->pending.empty()) return true;
+            if (s->pending.empty() || s->mem_blocked || s->pause_admission) return false;
+            for (Slot& sl : s->slots)
+                if (!sl.q) return true;
+            return false;
+        });
+        bool any_busy = false;
+        for (Slot& sl : s->slots) any_busy |= sl.q != nullptr;
+        if (s->stop && !any_busy && s->pending.empty()) return;
+        bool queued = false;
+        for (Slot& sl : s->slots)
+            if (slot_finished(sl)) {
+                sl.finishing = true;
+                s->jobs.emplace_back(false, &sl);
+                queued = true;
+            }
+        bool failed_any = false;
+        // admit in arrival order while a slot is free and the scratch fits
+        while (!s->pending.empty() && !s->pause_admission) {
+            Query* q = s->pending.front();
             DeviceGraph* g = q->graph;
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, sl->ev_start, sl->ev_end);
-            q->device_ms = ms;
-            std::memcpy(&q->counters, sl->h_tail, sizeof(RunCounters));
-            uint32_t last_flag = 0;
-            std::memcpy(&last_flag, sl->h_tail + kTailFlags + 4 * jump_flag_index(g->n), sizeof(uint32_t));
-            if (q->status == SCAN_OK && (q->counters.error_flags || last_flag)) {
-                q->status = SCAN_ERR_DEVICE;
-                q->error = "union-find did not finish within its limits";
-            }
-            if (q->status == SCAN_OK) {
-                std::memcpy(q->out_label, sl->h_res, g->n * sizeof(int32_t));
-                if (q->out_role) std::memcpy(q->out_role, sl->h_res + res_role_offset(g->n), g->n);
-            }
-        }
-        {
-            std::lock_guard<std::mutex> lock(s->mu);
-            for (Slot* sl : finished) {
-                Query* q = sl->q;
-                s->arena.release(sl->arena_off, sl->arena_bytes);
-                s->mem_blocked = false;
-                sl->q = nullptr;
+            const uint64_t need = run_scratch_bytes(g->n, g->E);
+            if (need > s->arena.size()) {   // can never fit
+                s->pending.pop_front();
+                q->status = SCAN_ERR_OUT_OF_MEMORY;
+                q->error = "query scratch exceeds the server's memory budget";
                 q->finished = Clock::now();
                 q->done = true;
                 ++s->totals.completed;
-                if (q->status != SCAN_OK) ++s->totals.failed;
+                ++s->totals.failed;
+                failed_any = true;
+                continue;
             }
-            // admit in arrival order while a slot is free and the scratch fits
-            while (!s->pending.empty() && !s->pause_admission) {
-                Query* q = s->pending.front();
-                DeviceGraph* g = q->graph;
-                const uint64_t need = run_scratch_bytes(g->n, g->E);
-                if (need > s->arena.size()) {   // can never fit
-                    s->pending.pop_front();
-                    q->status = SCAN_ERR_OUT_OF_MEMORY;
-                    q->error = "query scratch exceeds the server's memory budget";
-                    q->finished = Clock::now();
-                    q->done = true;
-                    ++s->totals.completed;
-                    ++s->totals.failed;
-                    finished.push_back(nullptr);   // waiters to wake
-                    continue;
-                }
-                Slot* free_slot = nullptr;
-                for (Slot& sl : s->slots)
-                    if (!sl.q) { free_slot = &sl; break; }
-                if (!free_slot) break;
-                uint64_t off = 0;
-                if (!s->arena.alloc(need, &off)) {
-                    s->mem_blocked = true;   // admitted again once a running query returns its block
-                    break;
-                }
-                s->pending.pop_front();
-                free_slot->q = q;
-                free_slot->arena_off = off;
-                free_slot->arena_bytes = need;
-                free_slot->gpu_done.store(false);
-                free_slot->launching = true;
-                q->admitted = Clock::now();
-                ++s->totals.admitted;
-                to_launch.push_back(free_slot);
+            Slot* free_slot = nullptr;
+            for (Slot& sl : s->slots)
+                if (!sl.q) { free_slot = &sl; break; }
+            if (!free_slot) break;
+            uint64_t off = 0;
+            if (!s->arena.alloc(need, &off)) {
+                s->mem_blocked = true;   // admitted again once a running query returns its block
+                break;
             }
+            s->pending.pop_front();
+            free_slot->q = q;
+            free_slot->arena_off = off;
+            free_slot->arena_bytes = need;
+            free_slot->gpu_done.store(false);
+            free_slot->launching = true;
+            q->admitted = Clock::now();
+            ++s->totals.admitted;
+            s->jobs.emplace_back(true, free_slot);
+            queued = true;
         }
-        if (!finished.empty()) s->cv_done.notify_all();
-        uint32_t launches = 0;
-        for (Slot* sl : to_launch) launches += launch_query(s, *sl, sl->q);
-        {
-            std::lock_guard<std::mutex> lock(s->mu);
-            for (Slot* sl : to_launch) sl->launching = false;
-            s->totals.kernel_launches += launches;
-            bool any_busy = false;
-            for (Slot& sl : s->slots) any_busy |= sl.q != nullptr;
-            if (!any_busy) s->cv_done.notify_all();   // a graph being added waits for idle slots
-        }
+        if (queued) s->cv_jobs.notify_all();
+        if (failed_any) s->cv_done.notify_all();
     }
 }
 
@@ -328,6 +355,9 @@ scan_status scan_server_create(int device, uint64_t memory_budget_bytes, uint32_
             return fail(SCAN_ERR_CUDA, "cannot create the server's streams");
         }
     }
+    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
+    const unsigned nworkers = std::min<unsigned>(max_in_flight, std::min(8u, hw / 2));
+    for (unsigned i = 0; i < std::max(1u, nworkers); ++i) s->workers.emplace_back(worker_loop, s.get());
     s->worker = std::thread(scheduler, s.get());
     *out = s.release();
     return SCAN_OK;
@@ -538,7 +568,14 @@ void scan_server_destroy(scan_server* s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
-    if (s->worker.joinable()) s->worker.join();
+    if (s->worker.joinable()) s->worker.join();   // returns once every slot is idle
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop_workers = true;
+    }
+    s->cv_jobs.notify_all();
+    for (std::thread& w : s->workers)
+        if (w.joinable()) w.join();
     cudaSetDevice(s->device);
     for (Slot& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);

@@ -73,3 +73,33 @@ def test_replay_trace():
                                    [q[3] for q in qs], arrivals)
         assert (st == 0).all() and (lat > 0).all()
         assert wall >= arrivals[-1]
+
+
+def boundary_graphs():
+    ring = [(i, (i + 1) % 20) for i in range(20)] + [(i, (i + 5) % 20) for i in range(20)]
+    v, u, a, b = 0, 1, 2, 3
+    prune = [(v, u), (v, a), (v, b), (u, a), (u, b)] + [(v, 4 + i) for i in range(12)]
+    twin = [(0, 1)] + [(0, 2 + i) for i in range(46339)] + [(1, 2 + i) for i in range(46339)]
+    return [sg.Graph.from_edges(20, ring), sg.Graph.from_edges(16, prune), sg.Graph.from_edges(46341, twin),
+            sg.Graph.sbm(16000, 8, 0.2, 0.002, 512, seed=7), sg.Graph.rmat(13, 16, seed=8)]
+
+
+def test_served_queries_at_predicate_boundaries():
+    """Served queries visit only the edges ranked similar at their eps (the ranking groups
+    edges by similarity threshold); at eps values on and around the exact and reference
+    boundaries every result must still equal scan_run."""
+    graphs = boundary_graphs()
+    eps_values = ["0", "0.1", "0.15", "0.2", "0.22", "0.4", "0.4999999", "0.5", "0.5000001", "0.7071", "0.99", "1",
+                  "1.5"]
+    with sg.Server(0, 512 << 20, 8) as srv:
+        ids = [srv.add_graph(g) for g in graphs]
+        qs = [(gi, e, mu, pred) for gi in range(len(graphs)) for e in eps_values for mu in (1, 2, 5)
+              for pred in (sg.PRED_EXACT, sg.PRED_REF_F64)]
+        tickets = [srv.submit(ids[gi], e, mu, pred) for gi, e, mu, pred in qs]
+        for t, (gi, e, mu, pred) in zip(tickets, qs):
+            label, role, info = srv.wait(t)
+            alone = graphs[gi].run(e, mu, pred)
+            assert np.array_equal(label, alone.label), (gi, e, mu, pred)
+            assert np.array_equal(role, alone.role), (gi, e, mu, pred)
+            assert info["num_similar_edges"] == alone.stats["num_similar_edges"], (gi, e, mu, pred)
+            assert info["num_clusters"] == alone.stats["num_clusters"], (gi, e, mu, pred)
