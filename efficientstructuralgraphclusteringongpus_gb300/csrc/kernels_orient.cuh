@@ -23,14 +23,17 @@ namespace scan {
 // (appended to big[] here), so one long list does not hold a warp for the whole pass.
 constexpr uint32_t kBigList = 2048;
 
-__global__ void k_count_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+// Vertices [v_begin, v_end) (the upload runs it chunk by chunk as the adjacency arrives).
+// Ids >= n are skipped here (the entry checks reject the graph before anything uses it).
+__global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ adj,
                               uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
                               const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
                               uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-    for (uint64_t v = warp; v < n; v += nwarps) {
+    for (uint64_t v = v_begin + warp; v < v_end; v += nwarps) {
         const uint32_t b = off[v], e = off[v + 1], dv = e - b;
         if (dv > kBigList) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = (uint32_t)v;
@@ -40,6 +43,7 @@ __global__ void k_count_lower(uint32_t n, const uint32_t* __restrict__ off, cons
         unsigned long long w = 0;
         for (uint32_t j = b + lane; j < e; j += 32) {
             const uint32_t u = adj[j];
+            if (u >= n) continue;
             const uint32_t du = off[u + 1] - off[u];
             if (precedes(du, u, dv, (uint32_t)v)) { ++c; w += du; }
             if (hot) tl += hot[u] >= hot_bits;
@@ -104,7 +108,8 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x
 __global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
                                   const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                                   uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
-                                  const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail) {
+                                  const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
+                                  uint32_t n) {
     __shared__ unsigned long long sh[32];
     const uint32_t nb = *nbig;
     for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
@@ -113,6 +118,7 @@ __global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32
         unsigned long long c = 0, w = 0, tl = 0;
         for (uint32_t j = b + threadIdx.x; j < e; j += blockDim.x) {
             const uint32_t u = adj[j];
+            if (u >= n) continue;   // rejected by the entry checks
             const uint32_t du = off[u + 1] - off[u];
             if (precedes(du, u, dv, v)) { ++c; w += du; }
             if (hot) tl += hot[u] >= hot_bits;
@@ -182,11 +188,13 @@ __global__ void k_mark_starts(uint32_t n, const uint32_t* __restrict__ off, uint
 
 // Entry j of some list: its value w is < n; j is not inside w's own list (that would be a
 // self-loop); unless j starts a list, w is above the previous entry.
-__global__ void k_check_entries(uint64_t m, uint32_t n, const uint32_t* __restrict__ off,
+// Entries [j_begin, j_end).
+__global__ void k_check_entries(uint64_t j_begin, uint64_t j_end, uint32_t n, const uint32_t* __restrict__ off,
                                 const uint32_t* __restrict__ adj, const uint32_t* __restrict__ starts,
                                 uint32_t* __restrict__ bad, uint32_t bad_id, uint32_t bad_loop, uint32_t bad_order) {
     uint32_t flags = 0;
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < m; j += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t j = j_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < j_end;
+         j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t w = adj[j];
         if (w >= n) { flags |= bad_id; continue; }
         if (off[w] <= j && j < off[w + 1]) flags |= bad_loop;
@@ -236,10 +244,14 @@ __global__ void k_hot_assign(uint32_t n, const uint32_t* __restrict__ off, uint3
     }
 }
 
-__global__ void k_map_adj(uint64_t m, const uint32_t* __restrict__ adj, const uint32_t* __restrict__ hot,
-                          uint32_t* __restrict__ radj) {
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < m; j += (uint64_t)gridDim.x * blockDim.x)
-        radj[j] = hot[adj[j]];
+// Entries [j_begin, j_end); ids >= n (rejected by the entry checks) map to 0xFFFFFFFF.
+__global__ void k_map_adj(uint64_t j_begin, uint64_t j_end, uint32_t n, const uint32_t* __restrict__ adj,
+                          const uint32_t* __restrict__ hot, uint32_t* __restrict__ radj) {
+    for (uint64_t j = j_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < j_end;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = adj[j];
+        radj[j] = w < n ? hot[w] : 0xFFFFFFFFu;
+    }
 }
 
 // ---- exclusive scan of uint32 counts (n items) into out[0..n], out[n] = total ----------

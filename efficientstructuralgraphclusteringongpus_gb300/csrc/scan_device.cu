@@ -330,53 +330,32 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     } else {
         SCAN_CUDA(cudaMemcpyAsync(d->off, off_host, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     }
-    if (adj_in_host_memory) {
-        std::memcpy(d->adj_host, adj_host, m * sizeof(uint32_t));
-        std::memset(d->adj_host + m, 0, kAdjPad * sizeof(uint32_t));
-    } else {
-        SCAN_CUDA(cudaMemcpyAsync(d->adj, adj_host, m * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-        SCAN_CUDA(cudaMemsetAsync(d->adj + m, 0, kAdjPad * sizeof(uint32_t), s));
-    }
-    SCAN_CUDA(cudaEventRecord(d->ev[1], s));
-
-    // Input checks first: the orientation kernels index by neighbour id.
+    // The offsets are checked first (every later kernel indexes lists by them), with the
+    // degree histogram of the hot-id assignment; both need only the offsets, so the host
+    // waits for those alone.
     k_check_offsets32<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->off, n, m, flags);
-    uint32_t bad = 0;
-    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    SCAN_CUDA(cudaStreamSynchronize(s));
-    if (bad) return fail(SCAN_ERR_FORMAT, "offsets are not a non-decreasing sequence from 0 to m");
-    {
-        uint32_t* starts = nullptr;
-        SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
-        SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s));
-        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, starts);
-        k_check_entries<<<grid_for(d.get(), m, 256), 256, 0, s>>>(m, d->n, d->off, d->adj, starts, flags, kBadId,
-                                                                  kBadSelfLoop, kBadOrder);
-        SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        SCAN_CUDA(cudaStreamSynchronize(s));
-    }
-    if (bad & kBadId) return fail(SCAN_ERR_FORMAT, "neighbour id >= n");
-    if (bad & kBadSelfLoop) return fail(SCAN_ERR_FORMAT, "self loop");
-    if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
 
     // Hot ids for the bitmap path: the kHotBits highest-degree vertices (by degree bin).
     // On by default wherever it applies: its pivots are never split, so the early stop of
-    // one-shot runs reaches the hubs too (R-MAT s22, eps 0.5: 36.5 ms against 46.9 ms for
-    // the hash classes; full counts for the cache: 66.9 against 62.8 ms).
-    // SCAN_GB300_BITMAP=off keeps the hash classes only; "tails-free" turns it on only when
-    // every vertex with an edge gets a hot id.
+    // one-shot runs reaches the hubs too.  SCAN_GB300_BITMAP=off keeps the hash classes
+    // only; "tails-free" turns it on only when every vertex with an edge gets a hot id.
     const char* knob = std::getenv("SCAN_GB300_BITMAP");
     const int mode = knob && !std::strcmp(knob, "off") ? 0 : knob && !std::strcmp(knob, "tails-free") ? 2 : 1;
     bool bitmap_path = mode != 0 && n + kHotBits < 0xFFFFFFF0ull && m > 0 && !adj_in_host_memory;
     uint32_t* hist = nullptr;
     std::vector<uint32_t> h(kDegBins, 0);
-    uint32_t min_bin = 1;                            // isolated vertices are never hot
     if (bitmap_path) {
         SCAN_TRY(dalloc(d.get(), &hist, kDegBins + 1));
         SCAN_CUDA(cudaMemsetAsync(hist, 0, (kDegBins + 1) * sizeof(uint32_t), s));
         k_deg_hist<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, hist);
         SCAN_CUDA(cudaMemcpyAsync(h.data(), hist, kDegBins * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        SCAN_CUDA(cudaStreamSynchronize(s));
+    }
+    uint32_t bad = 0;
+    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaStreamSynchronize(s));
+    if (bad) return fail(SCAN_ERR_FORMAT, "offsets are not a non-decreasing sequence from 0 to m");
+    uint32_t min_bin = 1;                            // isolated vertices are never hot
+    if (bitmap_path) {
         uint64_t acc = 0;
         for (uint32_t b = kDegBins; b-- > 1;) {
             if (acc + h[b] > kHotBits) { min_bin = b + 1; break; }
@@ -384,33 +363,106 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         }
         if (mode == 2 && min_bin > 1) bitmap_path = false;   // some vertex would have a tail
     }
+    uint32_t* starts = nullptr;
+    SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
+    uint32_t* big_list = nullptr;
+    SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
+    uint32_t* nbig = flags + 16;
     if (bitmap_path) {
         SCAN_TRY(dalloc(d.get(), &d->hot, n));
         SCAN_TRY(dalloc(d.get(), &d->radj, m + kAdjPad));
         SCAN_TRY(dalloc(d.get(), &d->tailc, n));
-        k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s>>>(d->n, d->off, min_bin, kHotBits, d->hot, hist + kDegBins);
-        k_map_adj<<<grid_for(d.get(), m, 256), 256, 0, s>>>(m, d->adj, d->hot, d->radj);
-        SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s));
     }
 
-    // Orientation: warps for short lists, CTAs for the lists k_count_lower sets aside.
-    uint32_t* big_list = nullptr;
-    SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
-    uint32_t* nbig = flags + 16;
-    SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s));
-    k_count_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, cnt, d->work, d->hot, kHotBits,
-                                                                d->tailc, big_list, nbig);
-    k_count_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, cnt, d->work, d->hot, kHotBits,
-                                                       d->tailc);
+    // The adjacency arrives in chunks of whole vertex ranges; each chunk's entry checks,
+    // hot-id mapping and orientation count run on a second stream while the next chunk is
+    // copied.  The count kernels skip ids >= n, so no host check has to come in between;
+    // the flags are read once, after the count.
+    cudaStream_t s2 = nullptr;
+    SCAN_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    constexpr int kMaxChunks = 4;
+    cudaEvent_t ev_chunk[kMaxChunks + 1] = {};
+    auto cleanup = [&] {
+        for (auto& e : ev_chunk)
+            if (e) cudaEventDestroy(e);
+        cudaStreamDestroy(s2);
+    };
+    const int chunks = (adj_in_host_memory || m < (16ull << 20)) ? 1 : kMaxChunks;
+    std::vector<uint32_t> vcut(chunks + 1, 0);
+    vcut[chunks] = (uint32_t)n;
+    auto off_at = [&](uint64_t v) -> uint64_t {
+        return off64 ? static_cast<const uint64_t*>(off_host)[v] : static_cast<const uint32_t*>(off_host)[v];
+    };
+    for (int c = 1; c < chunks; ++c) {            // first vertex whose list starts at or after c*m/chunks
+        uint64_t lo = vcut[c - 1], hi = n, target = m * (uint64_t)c / chunks;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) / 2;
+            if (off_at(mid) < target) lo = mid + 1; else hi = mid;
+        }
+        vcut[c] = (uint32_t)lo;
+    }
+    scan_status ost = SCAN_OK;
+    auto enqueue = [&]() -> scan_status {
+        for (auto& e : ev_chunk) SCAN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        // on s2, needing only the offsets (already on the device)
+        SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s2));
+        SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s2));
+        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, starts);
+        if (bitmap_path)
+            k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, min_bin, kHotBits, d->hot,
+                                                                  hist + kDegBins);
+        if (adj_in_host_memory) {
+            std::memcpy(d->adj_host, adj_host, m * sizeof(uint32_t));
+            std::memset(d->adj_host + m, 0, kAdjPad * sizeof(uint32_t));
+        } else {
+            SCAN_CUDA(cudaMemsetAsync(d->adj + m, 0, kAdjPad * sizeof(uint32_t), s));
+        }
+        for (int c = 0; c < chunks; ++c) {
+            const uint64_t j0 = off_at(vcut[c]), j1 = off_at(vcut[c + 1]);
+            if (!adj_in_host_memory && j1 > j0)
+                SCAN_CUDA(cudaMemcpyAsync(d->adj + j0, adj_host + j0, (j1 - j0) * sizeof(uint32_t),
+                                          cudaMemcpyHostToDevice, s));
+            SCAN_CUDA(cudaEventRecord(ev_chunk[c], s));
+            SCAN_CUDA(cudaStreamWaitEvent(s2, ev_chunk[c], 0));
+            if (j1 > j0) {
+                k_check_entries<<<grid_for(d.get(), j1 - j0, 256), 256, 0, s2>>>(j0, j1, d->n, d->off, d->adj, starts,
+                                                                                 flags, kBadId, kBadSelfLoop, kBadOrder);
+                if (bitmap_path)
+                    k_map_adj<<<grid_for(d.get(), j1 - j0, 256), 256, 0, s2>>>(j0, j1, d->n, d->adj, d->hot, d->radj);
+            }
+            const uint32_t nv = vcut[c + 1] - vcut[c];
+            if (nv)
+                k_count_lower<<<grid_for(d.get(), (uint64_t)nv * 32, 256), 256, 0, s2>>>(
+                    d->n, vcut[c], vcut[c + 1], d->off, d->adj, cnt, d->work, d->hot, kHotBits, d->tailc, big_list, nbig);
+        }
+        SCAN_CUDA(cudaEventRecord(d->ev[1], s));   // end of the copies
+        if (bitmap_path) SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s2));
+        k_count_lower_big<<<d->num_sms * 2, 1024, 0, s2>>>(big_list, nbig, d->off, d->adj, cnt, d->work, d->hot,
+                                                            kHotBits, d->tailc, d->n);
+        SCAN_CUDA(cudaEventRecord(ev_chunk[kMaxChunks], s2));
+        SCAN_CUDA(cudaStreamWaitEvent(s, ev_chunk[kMaxChunks], 0));   // back to one stream
+        return SCAN_OK;
+    };
+    ost = enqueue();
+    if (ost != SCAN_OK) {
+        cudaStreamSynchronize(s2);
+        cleanup();
+        return ost;
+    }
+    cleanup();   // pending work on s2 completes; s waits on its last event
     SCAN_TRY(device_scan(d.get(), cnt, n, d->lo_off, d->scratch));
     uint32_t E32 = 0;
     SCAN_CUDA(cudaMemcpyAsync(&E32, d->lo_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SCAN_CUDA(cudaMemcpyAsync(&bad, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
+    if (bad & kBadId) return fail(SCAN_ERR_FORMAT, "neighbour id >= n");
+    if (bad & kBadSelfLoop) return fail(SCAN_ERR_FORMAT, "self loop");
+    if (bad & kBadOrder) return fail(SCAN_ERR_FORMAT, "neighbour list not sorted strictly ascending");
     d->E = E32;
     if (d->E * 2 != m) return fail(SCAN_ERR_FORMAT, "graph is not symmetric (lower entries * 2 != m)");
     SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
     SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
-    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
+    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);   // checked input
     k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
     SCAN_CUDA(cudaGetLastError());
 

@@ -339,3 +339,37 @@ def test_reference_kernels_admissible(scale, seed, eps, mu):
     # and our engine's answer is admissible in the same sense
     res = g.run(eps, mu, REF)
     assert oracle.check_admissible(g.offsets(), g.adjacency(), eps, mu, REF, res.label) == viol
+
+
+# ---- uploads of 16M+ entries arrive in four chunks checked and oriented as they land ----
+def test_chunked_upload_matches_oracle():
+    g = sg.Graph.rmat(20, 16, seed=12)
+    assert g.m >= (16 << 20)
+    assert_same_as_oracle(g, "0.4", 3, REF)
+    cn, _ = g.common_neighbors()
+    assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
+
+
+@pytest.mark.parametrize("where", [0.1, 0.55, 0.999])
+@pytest.mark.parametrize("fault", ["id", "self_loop", "order"])
+def test_chunked_upload_rejects_bad_entries(where, fault):
+    g = sg.Graph.rmat(20, 16, seed=12)
+    off = g.offsets().astype(np.uint32)
+    adj = g.adjacency().astype(np.int32).copy()
+    deg = np.diff(off.astype(np.int64))
+    v = int(np.searchsorted(off, int(where * len(adj)), side="right")) - 1
+    while deg[v] < 2:
+        v += 1
+    b = int(off[v])
+    if fault == "id":
+        adj[b] = g.n + 5
+        msg = "neighbour id"
+    elif fault == "self_loop":
+        adj[b] = v
+        msg = "self loop"                      # reported before any order violation it causes
+    else:
+        adj[b], adj[b + 1] = adj[b + 1], adj[b]
+        msg = "sorted"
+    with pytest.raises(sg.ScanError) as e:
+        sg.GPUScan(off, adj, 0.5, 2)
+    assert msg in str(e.value)
