@@ -25,11 +25,20 @@ constexpr uint32_t kBigList = 2048;
 
 // Vertices [v_begin, v_end) (the upload runs it chunk by chunk as the adjacency arrives).
 // Ids >= n are skipped here (the entry checks reject the graph before anything uses it).
+// lowbits gets one bit per adjacency entry, set for the lower neighbours, so the fill
+// pass reads the decision instead of gathering both degrees again.
+__device__ __forceinline__ void set_low_bits(uint32_t* bits, uint32_t j0, uint32_t mask) {
+    if (!mask) return;
+    const uint32_t sh = j0 & 31u;
+    atomicOr(&bits[j0 >> 5], mask << sh);
+    if (sh) atomicOr(&bits[(j0 >> 5) + 1], mask >> (32u - sh));
+}
+
 __global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ adj,
                               uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
                               const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
-                              uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
+                              uint32_t* __restrict__ big, uint32_t* __restrict__ nbig, uint32_t* __restrict__ lowbits) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
@@ -41,12 +50,20 @@ __global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, cons
         }
         uint32_t c = 0, tl = 0;
         unsigned long long w = 0;
-        for (uint32_t j = b + lane; j < e; j += 32) {
-            const uint32_t u = adj[j];
-            if (u >= n) continue;
-            const uint32_t du = off[u + 1] - off[u];
-            if (precedes(du, u, dv, (uint32_t)v)) { ++c; w += du; }
-            if (hot) tl += hot[u] >= hot_bits;
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool low = false;
+            if (j < e) {
+                const uint32_t u = adj[j];
+                if (u < n) {
+                    const uint32_t du = off[u + 1] - off[u];
+                    low = precedes(du, u, dv, (uint32_t)v);
+                    if (low) { ++c; w += du; }
+                    if (hot) tl += hot[u] >= hot_bits;
+                }
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
+            if (lane == 0) set_low_bits(lowbits, j0, mask);
         }
         c = __reduce_add_sync(0xFFFFFFFFu, c);
         tl = __reduce_add_sync(0xFFFFFFFFu, tl);
@@ -61,8 +78,8 @@ __global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, cons
 
 // Warp per vertex: write the lower neighbours of v at lo_off[v] in ascending id order.
 __global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                             const uint32_t* __restrict__ lo_off, uint32_t* __restrict__ lo_adj,
-                             uint32_t* __restrict__ lo_src) {
+                             const uint32_t* __restrict__ lo_off, const uint32_t* __restrict__ lowbits,
+                             uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
@@ -77,7 +94,7 @@ __global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const
             uint32_t u = 0;
             if (j < e) {
                 u = adj[j];
-                low = precedes(off[u + 1] - off[u], u, dv, (uint32_t)v);
+                low = (lowbits[j >> 5] >> (j & 31u)) & 1u;
             }
             const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
             if (low) {
@@ -109,19 +126,27 @@ __global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32
                                   const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                                   uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
                                   const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
-                                  uint32_t n) {
+                                  uint32_t n, uint32_t* __restrict__ lowbits) {
     __shared__ unsigned long long sh[32];
     const uint32_t nb = *nbig;
     for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
         const uint32_t v = big[i];
         const uint32_t b = off[v], e = off[v + 1], dv = e - b;
         unsigned long long c = 0, w = 0, tl = 0;
-        for (uint32_t j = b + threadIdx.x; j < e; j += blockDim.x) {
-            const uint32_t u = adj[j];
-            if (u >= n) continue;   // rejected by the entry checks
-            const uint32_t du = off[u + 1] - off[u];
-            if (precedes(du, u, dv, v)) { ++c; w += du; }
-            if (hot) tl += hot[u] >= hot_bits;
+        for (uint32_t j0 = b + (threadIdx.x & ~31u); j0 < e; j0 += blockDim.x) {   // warp-uniform bounds
+            const uint32_t j = j0 + (threadIdx.x & 31u);
+            bool low = false;
+            if (j < e) {
+                const uint32_t u = adj[j];
+                if (u < n) {                 // ids >= n: rejected by the entry checks
+                    const uint32_t du = off[u + 1] - off[u];
+                    low = precedes(du, u, dv, v);
+                    if (low) { ++c; w += du; }
+                    if (hot) tl += hot[u] >= hot_bits;
+                }
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
+            if ((threadIdx.x & 31u) == 0) set_low_bits(lowbits, j0, mask);
         }
         c = block_sum_u64(c, sh);
         w = block_sum_u64(w, sh);
@@ -138,8 +163,8 @@ __global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32
 // at a time (block-wide exclusive scan of the flags).
 __global__ void k_fill_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
                                  const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                                 const uint32_t* __restrict__ lo_off, uint32_t* __restrict__ lo_adj,
-                                 uint32_t* __restrict__ lo_src) {
+                                 const uint32_t* __restrict__ lo_off, const uint32_t* __restrict__ lowbits,
+                                 uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
     __shared__ uint32_t warp_cnt[32];
     __shared__ uint32_t tile_base;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -155,7 +180,7 @@ __global__ void k_fill_lower_big(const uint32_t* __restrict__ big, const uint32_
             uint32_t u = 0;
             if (j < e) {
                 u = adj[j];
-                low = precedes(off[u + 1] - off[u], u, dv, v);
+                low = (lowbits[j >> 5] >> (j & 31u)) & 1u;
             }
             const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
             if (lane == 0) warp_cnt[wid] = __popc(mask);

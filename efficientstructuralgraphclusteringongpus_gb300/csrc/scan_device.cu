@@ -367,6 +367,8 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
     uint32_t* big_list = nullptr;
     SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
+    uint32_t* lowbits = nullptr;                               // one bit per entry: lower neighbour
+    SCAN_TRY(dalloc(d.get(), &lowbits, m / 32 + 2));
     uint32_t* nbig = flags + 16;
     if (bitmap_path) {
         SCAN_TRY(dalloc(d.get(), &d->hot, n));
@@ -407,6 +409,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         // on s2, needing only the offsets (already on the device)
         SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s2));
         SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s2));
+        SCAN_CUDA(cudaMemsetAsync(lowbits, 0, (m / 32 + 2) * sizeof(uint32_t), s2));
         k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, starts);
         if (bitmap_path)
             k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, min_bin, kHotBits, d->hot,
@@ -433,12 +436,13 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
             const uint32_t nv = vcut[c + 1] - vcut[c];
             if (nv)
                 k_count_lower<<<grid_for(d.get(), (uint64_t)nv * 32, 256), 256, 0, s2>>>(
-                    d->n, vcut[c], vcut[c + 1], d->off, d->adj, cnt, d->work, d->hot, kHotBits, d->tailc, big_list, nbig);
+                    d->n, vcut[c], vcut[c + 1], d->off, d->adj, cnt, d->work, d->hot, kHotBits, d->tailc, big_list, nbig,
+                    lowbits);
         }
         SCAN_CUDA(cudaEventRecord(d->ev[1], s));   // end of the copies
         if (bitmap_path) SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s2));
         k_count_lower_big<<<d->num_sms * 2, 1024, 0, s2>>>(big_list, nbig, d->off, d->adj, cnt, d->work, d->hot,
-                                                            kHotBits, d->tailc, d->n);
+                                                            kHotBits, d->tailc, d->n, lowbits);
         SCAN_CUDA(cudaEventRecord(ev_chunk[kMaxChunks], s2));
         SCAN_CUDA(cudaStreamWaitEvent(s, ev_chunk[kMaxChunks], 0));   // back to one stream
         return SCAN_OK;
@@ -462,8 +466,10 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (d->E * 2 != m) return fail(SCAN_ERR_FORMAT, "graph is not symmetric (lower entries * 2 != m)");
     SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
     SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
-    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);   // checked input
-    k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, d->lo_adj, d->lo_src);
+    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, lowbits, d->lo_adj,
+                                                                d->lo_src);
+    k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, lowbits, d->lo_adj,
+                                                      d->lo_src);
     SCAN_CUDA(cudaGetLastError());
 
     // Task plan.
