@@ -58,7 +58,8 @@ struct DeviceGraph {
     unsigned long long* work = nullptr;
     unsigned long long* cn_ctr = nullptr;
     uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel
-    bool has_split = false;                // the plan splits some pivot into chunks   // last launch_cn: [0] 16-byte list words read, [1] edges counted
+    bool has_split = false;                // the plan splits some pivot into chunks
+    float* tau = nullptr;                  // served graphs: 2E similarity thresholds (k_tau)   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;
     uint32_t nsmall = 0;
     scan::CnTask* big[scan::kNumBigClasses] = {};
@@ -123,6 +124,8 @@ struct BatchParams {
 // No host synchronisation.  bp (may be null) gives per-graph parameters.
 scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream_t s, const PredParams& pp, int mu,
                            uint32_t* launches, const BatchParams* bp = nullptr, bool predicate_done = false);
+// Cache the similarity threshold of every edge of a graph with full counts (served graphs).
+scan_status compute_tau(DeviceGraph* d);
 // eps text + mode -> predicate parameters.
 scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode);
 

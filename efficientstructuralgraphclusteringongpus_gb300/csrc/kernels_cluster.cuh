@@ -53,6 +53,70 @@ __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, con
     }
 }
 
+// Served queries on cached counts: each edge's similarity threshold, precomputed once per
+// graph, so the predicate is one compare per edge.  Edge e is similar at eps exactly when
+// eps^2 <= tau(e): tau_x = (t+2)^2 / ((du+1)(dv+1)) for the exact test, tau_r =
+// min((du+1)/(dv+1), t2/((du+1)(dv+1))) for the reference's doubles (t2 the int square;
+// -1 when it wraps negative: never similar).  Both are monotone in eps because IEEE
+// products are.  Stored as floats; an edge whose tau lies within a relative kTauBand of
+// eps^2 (float rounding is 6e-8) is decided by the predicate itself.
+constexpr double kTauBand = 1e-6;
+
+__global__ void k_tau(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                      const uint32_t* __restrict__ off, const uint32_t* __restrict__ cn, float* __restrict__ tau) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t u = lo_adj[e], v = lo_src[e];
+        const uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v], t = cn[e];
+        const double du1 = (double)(du + 1u), dv1 = (double)(dv + 1u);
+        const double a = (double)(t + 2u);
+        tau[e] = (float)(a * a / (du1 * dv1));
+        const int32_t t2 = (int32_t)((t + 2u) * (t + 2u));
+        tau[E + e] = t2 < 0 ? -1.0f : (float)fmin(du1 / dv1, (double)t2 / (du1 * dv1));
+    }
+}
+
+// k_predicate for a served graph: the cached thresholds decide every edge outside the
+// band; the disagreement counter is not kept (the server does not report it).
+__global__ void k_predicate_tau(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
+                                const uint32_t* __restrict__ off, const uint32_t* __restrict__ cn,
+                                const float* __restrict__ tau, PredParams pp, uint8_t* __restrict__ sim,
+                                int32_t* __restrict__ sd, RunCounters* __restrict__ ctr) {
+    const uint32_t lane = threadIdx.x & 31;
+    const float* tm = tau + (pp.mode ? E : 0);
+    double theta;
+    if (pp.mode) theta = pp.eps * pp.eps;
+    else theta = pp.q == 0 ? 2.0 : ((double)pp.p / (double)pp.q) * ((double)pp.p / (double)pp.q);
+    const double hi = theta * (1.0 + kTauBand), lo = theta * (1.0 - kTauBand);
+    unsigned long long nsim = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t e0 = (uint64_t)blockIdx.x * blockDim.x; e0 < E; e0 += stride) {
+        const uint64_t e = e0 + threadIdx.x;
+        bool s = false;
+        uint32_t v = kEmpty;
+        if (e < E) {
+            const double tv = (double)tm[e];
+            if (tv >= hi) {
+                s = true;
+            } else if (tv > lo || (theta == 0.0 && tv == 0.0)) {
+                const uint32_t u = lo_adj[e], w = lo_src[e];
+                const uint32_t du = off[u + 1] - off[u], dw = off[w + 1] - off[w];
+                s = pp.mode ? ref_f64_similar(cn[e], du, dw, pp.eps) : exact_similar(cn[e], du, dw, pp.p, pp.q);
+            }
+            sim[e] = s;
+            if (s) {
+                v = lo_src[e];
+                atomicAdd(&sd[lo_adj[e]], 1);
+                ++nsim;
+            }
+        }
+        const uint32_t key = s ? v : kEmpty;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (s && (__ffs(peers) - 1) == (int)lane) atomicAdd(&sd[v], __popc(peers));
+    }
+    for (int o = 16; o > 0; o >>= 1) nsim += __shfl_xor_sync(0xFFFFFFFFu, nsim, o);
+    if (lane == 0 && nsim) atomicAdd(&ctr->similar_edges, nsim);
+}
+
 // parent[v] = v for cores, -1 otherwise; border/neighbour label ranges reset.  Batched
 // runs pass vgid[] and per-graph gmu[].
 __global__ void k_core_init(uint32_t n, const int32_t* __restrict__ sd, int mu, const uint32_t* __restrict__ vgid,

@@ -618,8 +618,11 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     ++*launches;
     const uint32_t* vgid = bp ? bp->vgid : nullptr;
     if (!predicate_done) {
-        k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr, r.sim,
-                                     r.sd, r.ctr);
+        if (d->tau && !bp && d->cn_valid)
+            k_predicate_tau<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, d->tau, pp, r.sim, r.sd, r.ctr);
+        else
+            k_predicate<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, d->off, d->cn, pp, vgid, bp ? bp->gpp : nullptr,
+                                         r.sim, r.sd, r.ctr);
         ++*launches;
     }
     k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax,
@@ -638,6 +641,14 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     k_neighbour_labels<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.lab, r.nmin, r.nmax, r.ctr);
     k_finalize<<<gn, T, 0, s>>>(n, r.parent, r.bmin, r.bmax, r.nmin, r.nmax, r.label, r.role, r.ctr);
     *launches += 6;
+    SCAN_CUDA(cudaGetLastError());
+    return SCAN_OK;
+}
+
+scan_status compute_tau(DeviceGraph* d) {
+    if (!d->tau) SCAN_TRY(dalloc(d, &d->tau, 2 * std::max<uint64_t>(d->E, 1)));
+    if (d->E) k_tau<<<grid_for(d, d->E, 256), 256, 0, d->stream>>>(d->E, d->lo_adj, d->lo_src, d->off, d->cn, d->tau);
+    SCAN_CUDA(cudaStreamSynchronize(d->stream));
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
 }

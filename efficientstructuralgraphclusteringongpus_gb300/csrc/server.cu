@@ -373,6 +373,7 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
     st = launch_cn(d, &launches);
     if (st == SCAN_OK && cudaStreamSynchronize(d->stream) != cudaSuccess)
         st = fail(SCAN_ERR_CUDA, "similarity stage failed while adding a graph");
+    if (st == SCAN_OK) st = compute_tau(d);   // queries then test each edge with one compare
     if (st != SCAN_OK) {
         device_graph_free(d);
         return st;
