@@ -256,7 +256,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
 //     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
 constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
 constexpr int kWordsInFlight = 2;        // hash kernel (48+ registers would cost occupancy)
-constexpr int kWordsInFlightBitmap = 4;  // bitmap kernel (one CTA per SM: registers to spare)
+constexpr int kWordsInFlightBitmap = 6;  // bitmap kernel: one CTA per SM, 64 registers at 6 (s22: -0.6 ms against 4)
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
     if (hi <= lo) return 0u;
