@@ -228,7 +228,7 @@ scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const 
 void scan_batch_free(scan_batch* b);
 
 /* ---- serving: queries on resident graphs with cached common-neighbour counts ---------
- * Serves the benchmark spec's serving pattern; the reference has no serving loop.  Each graph
+ * A request loop over resident graphs; the reference has no serving loop.  Each graph
  * added is uploaded once and its exact cn[] computed once; a query (graph, eps, mu) then runs
  * only the cluster stage.  Queries are admitted in arrival order when one of max_in_flight
  * stream slots is free and their scratch fits memory_budget_bytes (reserved on the device at
