@@ -3,7 +3,7 @@
 // TEST INFRASTRUCTURE ONLY (part of the oracle; the product never loads it).
 //
 // The kernels come from GPUSCAN++/GPUScan.cu compiled unmodified into a cubin
-// (oracle/build_ref.py writes oracle/_ref/gpuscan_ref.cubin).  This file replays the host
+// (oracle/build.py writes oracle/_ref/gpuscan_ref.cubin).  This file replays the host
 // sequence of GPUScan() (GPUSCAN++/GPUScan.cu:800-1009): the same allocations and copies,
 // the same eight kernel launches in the same order with the same grid shapes
 // (TOTALTHDCOUNT = 65536 threads; 512-thread "ii" and 128-thread "cc" blocks, :18-21,

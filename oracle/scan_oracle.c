@@ -1,15 +1,15 @@
 /*
  * scan_oracle.c -- CPU restatement of GPUSCAN++'s SCAN semantics.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA engine: only tests/,
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA engine: only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.  The product library
  * (libscan_gb300.so) never links, loads or calls it.
  *
  * Pinning: the reference ships no tests or golden vectors.  This restatement is pinned
  * (a) against the reference's own host orientation (GPUSCAN++/Graph.cpp:52-141, compiled
- *     from the reference sources by oracle/build_ref.py) on the CPU, and
+ *     from the reference sources by oracle/build.py) on the CPU, and
  * (b) against the reference's own kernels (GPUSCAN++/GPUScan.cu, compiled to a cubin by
- *     oracle/build_ref.py and driven in the reference's launch order by
+ *     oracle/build.py and driven in the reference's launch order by
  *     oracle/ref_harness.cu) on the GPU.
  *
  * Semantics restated (reference file:line):
