@@ -76,37 +76,6 @@ __global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, cons
     }
 }
 
-// Warp per vertex: write the lower neighbours of v at lo_off[v] in ascending id order.
-__global__ void k_fill_lower(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                             const uint32_t* __restrict__ lo_off, const uint32_t* __restrict__ lowbits,
-                             uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
-    for (uint64_t v = warp; v < n; v += nwarps) {
-        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
-        if (dv > kBigList) continue;
-        uint32_t pos = lo_off[v];
-        for (uint32_t j0 = b; j0 < e; j0 += 32) {
-            const uint32_t j = j0 + lane;
-            bool low = false;
-            uint32_t u = 0;
-            if (j < e) {
-                u = adj[j];
-                low = (lowbits[j >> 5] >> (j & 31u)) & 1u;
-            }
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
-            if (low) {
-                const uint32_t p = pos + __popc(mask & lt);
-                lo_adj[p] = u;
-                lo_src[p] = (uint32_t)v;
-            }
-            pos += __popc(mask);
-        }
-    }
-}
-
 // CTA per long list (vertices collected by k_count_lower): the same counts with a block
 // reduction.
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x, unsigned long long* sh) {
@@ -159,55 +128,93 @@ __global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32
     }
 }
 
-// CTA per long list: lower neighbours written in list order, one tile of blockDim entries
-// at a time (block-wide exclusive scan of the flags).
-__global__ void k_fill_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
-                                 const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                                 const uint32_t* __restrict__ lo_off, const uint32_t* __restrict__ lowbits,
-                                 uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
-    __shared__ uint32_t warp_cnt[32];
-    __shared__ uint32_t tile_base;
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint32_t nb = *nbig;
-    for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
-        const uint32_t v = big[i];
-        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
-        if (threadIdx.x == 0) tile_base = lo_off[v];
-        __syncthreads();
-        for (uint32_t j0 = b; j0 < e; j0 += blockDim.x) {
-            const uint32_t j = j0 + threadIdx.x;
-            bool low = false;
-            uint32_t u = 0;
-            if (j < e) {
-                u = adj[j];
-                low = (lowbits[j >> 5] >> (j & 31u)) & 1u;
-            }
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
-            if (lane == 0) warp_cnt[wid] = __popc(mask);
-            __syncthreads();
-            uint32_t before = tile_base, total = 0;
-            for (uint32_t w = 0; w < nw; ++w) {
-                if (w < wid) before += warp_cnt[w];
-                total += warp_cnt[w];
-            }
-            if (low) {
-                const uint32_t p = before + __popc(mask & ((1u << lane) - 1u));
-                lo_adj[p] = u;
-                lo_src[p] = v;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) tile_base += total;
-            __syncthreads();
+// ---- input checks, entry-parallel -----------------------------------------------------------
+// starts: one bit per adjacency position, set where a non-empty list begins.
+// tile_v[k]: the vertex whose list holds entry k * kFillTile (the fill pass's tile map).
+constexpr uint32_t kFillTile = 2048;
+__global__ void k_mark_starts(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ starts,
+                              uint32_t* __restrict__ tile_v) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = off[v], e = off[v + 1];
+        if (e > b) {
+            atomicOr(&starts[b >> 5], 1u << (b & 31u));
+            for (uint64_t k = (b + (uint64_t)kFillTile - 1) / kFillTile; k * kFillTile < e; ++k)
+                tile_v[k] = (uint32_t)v;
         }
     }
 }
 
-// ---- input checks, entry-parallel -----------------------------------------------------------
-// starts: one bit per adjacency position, set where a non-empty list begins.
-__global__ void k_mark_starts(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ starts) {
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = off[v];
-        if (off[v + 1] > b) atomicOr(&starts[b >> 5], 1u << (b & 31u));
+// Tile of kFillTile entries per CTA iteration: write the lower neighbours (bit set in
+// lowbits) in adjacency order.  Entry j goes to wpre[j / 32] + (lower bits before j in its
+// word), wpre being the exclusive scan of the words' popcounts; in adjacency order the
+// lower entries of v are exactly lo_adj[lo_off[v], lo_off[v+1]).  The pivot of each
+// entry comes from the tile's owner map: the list starts inside the tile are scattered
+// into shared memory and an inclusive max-scan spreads each vertex over its entries.
+// Entry-parallel, so a hub list costs what any other entries cost.
+constexpr int kFillThreads = 256;
+__device__ __forceinline__ uint32_t fill_slot(uint32_t i) { return i + (i >> 5); }   // bank skew
+
+__global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_t m, uint32_t E,
+                                                             const uint32_t* __restrict__ off,
+                                                             const uint32_t* __restrict__ adj,
+                                                             const uint32_t* __restrict__ tile_v,
+                                                             const uint32_t* __restrict__ lowbits,
+                                                             const uint32_t* __restrict__ wpre,
+                                                             uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
+    constexpr int kPer = kFillTile / kFillThreads;
+    __shared__ uint32_t owner[kFillTile + kFillTile / 32];
+    __shared__ uint32_t warp_max[kFillThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint64_t ntiles = (m + kFillTile - 1) / kFillTile;
+    for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const uint64_t j0 = k * kFillTile;
+        const uint32_t len = (uint32_t)min((uint64_t)kFillTile, m - j0);
+        const uint32_t v0 = tile_v[k];
+        const uint32_t v1 = k + 1 < ntiles ? tile_v[k + 1] : n - 1;   // owner of the next tile's first entry
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) owner[fill_slot(q * kFillThreads + tid)] = 0;
+        __syncthreads();
+        if (tid == 0) owner[0] = v0;
+        // Every list that starts inside the tile belongs to a vertex in (v0, v1].
+        for (uint64_t v = (uint64_t)v0 + 1 + tid; v <= v1; v += kFillThreads) {
+            const uint32_t b = off[v];
+            if (b < j0 + len && off[v + 1] > b) owner[fill_slot((uint32_t)(b - j0))] = (uint32_t)v;
+        }
+        __syncthreads();
+        uint32_t x[kPer], run = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            run = max(run, owner[fill_slot(tid * kPer + q)]);
+            x[q] = run;
+        }
+        uint32_t incl = run;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+            if (lane >= (uint32_t)s) incl = max(incl, y);
+        }
+        uint32_t pre = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if (lane == 0) pre = 0;
+        if (lane == 31) warp_max[wid] = incl;
+        __syncthreads();
+        for (uint32_t w = 0; w < wid; ++w) pre = max(pre, warp_max[w]);
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) owner[fill_slot(tid * kPer + q)] = max(pre, x[q]);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint32_t i = q * kFillThreads + tid;
+            if (i < len) {
+                const uint64_t j = j0 + i;
+                const uint32_t word = lowbits[j >> 5], bit = (uint32_t)j & 31u;
+                const uint32_t p = wpre[j >> 5] + __popc(word & ((1u << bit) - 1u));
+                if (((word >> bit) & 1u) && p < E) {   // p < E always: the bits are the counted entries
+                    lo_adj[p] = adj[j];
+                    lo_src[p] = owner[fill_slot(i)];
+                }
+            }
+        }
+        __syncthreads();   // the owner map is reset for the next tile
     }
 }
 
@@ -310,6 +317,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* w
     return r;
 }
 
+// kPopc: the items are the popcounts of the input words (the fill pass's word prefix).
+template <bool kPopc>
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in, uint64_t n,
                                                              uint32_t* __restrict__ out, uint32_t* __restrict__ sums) {
     __shared__ uint32_t warp_sums[32];
@@ -319,7 +328,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __r
     uint32_t t = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        v[i] = (base + i < n) ? in[base + i] : 0u;
+        v[i] = (base + i < n) ? (kPopc ? (uint32_t)__popc(in[base + i]) : in[base + i]) : 0u;
         t += v[i];
     }
     uint32_t ex = block_exclusive_scan(t, warp_sums, &total);

@@ -234,11 +234,16 @@ static int grid_for_n(int num_sms, uint64_t items, int threads, int per_sm = 8) 
     return (int)std::max<uint64_t>(g, 1);
 }
 
-// Exclusive scan of cnt[0..n) into out[0..n] on d->stream (out[n] = total).
-static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, uint32_t* out, uint32_t* sums) {
+// Exclusive scan of cnt[0..n) into out[0..n] on d->stream (out[n] = total); with popc,
+// of the popcounts of cnt's words.  sums: one slot per kScanTile items.
+static scan_status device_scan(DeviceGraph* d, const uint32_t* cnt, uint64_t n, uint32_t* out, uint32_t* sums,
+                               bool popc = false) {
     const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles > 0) {
-        k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, d->stream>>>(cnt, n, out, sums);
+        if (popc)
+            k_scan_tiles<true><<<(unsigned)tiles, kScanThreads, 0, d->stream>>>(cnt, n, out, sums);
+        else
+            k_scan_tiles<false><<<(unsigned)tiles, kScanThreads, 0, d->stream>>>(cnt, n, out, sums);
         k_scan_sums<<<1, kScanThreads, 0, d->stream>>>(sums, (uint32_t)tiles, out + n);
         k_scan_add<<<grid_for(d, n, 256), 256, 0, d->stream>>>(out, n, sums);
     } else {
@@ -363,8 +368,11 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         }
         if (mode == 2 && min_bin > 1) bitmap_path = false;   // some vertex would have a tail
     }
-    uint32_t* starts = nullptr;
+    uint32_t* starts = nullptr;                                 // later: the fill pass's word prefix
     SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
+    const uint64_t fill_tiles = (m + kFillTile - 1) / kFillTile;
+    uint32_t* tile_v = nullptr;
+    SCAN_TRY(dalloc(d.get(), &tile_v, fill_tiles + 1));
     uint32_t* big_list = nullptr;
     SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
     uint32_t* lowbits = nullptr;                               // one bit per entry: lower neighbour
@@ -410,7 +418,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s2));
         SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s2));
         SCAN_CUDA(cudaMemsetAsync(lowbits, 0, (m / 32 + 2) * sizeof(uint32_t), s2));
-        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, starts);
+        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, starts, tile_v);
         if (bitmap_path)
             k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, min_bin, kHotBits, d->hot,
                                                                   hist + kDegBins);
@@ -466,10 +474,14 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (d->E * 2 != m) return fail(SCAN_ERR_FORMAT, "graph is not symmetric (lower entries * 2 != m)");
     SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
     SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
-    k_fill_lower<<<grid_for(d.get(), n * 32, 256), 256, 0, s>>>(d->n, d->off, d->adj, d->lo_off, lowbits, d->lo_adj,
-                                                                d->lo_src);
-    k_fill_lower_big<<<d->num_sms * 2, 1024, 0, s>>>(big_list, nbig, d->off, d->adj, d->lo_off, lowbits, d->lo_adj,
-                                                      d->lo_src);
+    if (fill_tiles) {   // word prefix of the lower bits (into the spent start marks), then the fill
+        const uint64_t nwords = (m + 31) / 32;
+        uint32_t* wsums = nullptr;
+        SCAN_TRY(dalloc(d.get(), &wsums, (nwords + kScanTile - 1) / kScanTile + 1));
+        SCAN_TRY(device_scan(d.get(), lowbits, nwords, starts, wsums, true));
+        k_fill_tiles<<<grid_for(d.get(), fill_tiles * kFillThreads, kFillThreads), kFillThreads, 0, s>>>(
+            d->n, m, (uint32_t)d->E, d->off, d->adj, tile_v, lowbits, starts, d->lo_adj, d->lo_src);
+    }
     SCAN_CUDA(cudaGetLastError());
 
     // Task plan.
@@ -492,7 +504,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (st) {
         st->ms_h2d = ev_ms(d->ev[0], d->ev[1]);
         st->ms_orient = ev_ms(d->ev[1], d->ev[2]);
-        st->kernel_launches += 13 + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
+        st->kernel_launches += 11 + (fill_tiles ? 4 : 0) + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
     }
     *out = d.release();
     return SCAN_OK;
