@@ -17,143 +17,162 @@
 
 namespace scan {
 
-// Warp per vertex: number of lower neighbours and their total degree; with hot ids
-// (may be null), also the number of non-hot neighbours ("tail", bitmap path).
-// Vertices with more than kBigList entries are left to the CTA-per-vertex kernels below
-// (appended to big[] here), so one long list does not hold a warp for the whole pass.
-constexpr uint32_t kBigList = 2048;
-
-// Vertices [v_begin, v_end) (the upload runs it chunk by chunk as the adjacency arrives).
-// Ids >= n are skipped here (the entry checks reject the graph before anything uses it).
-// lowbits gets one bit per adjacency entry, set for the lower neighbours, so the fill
-// pass reads the decision instead of gathering both degrees again.
-__device__ __forceinline__ void set_low_bits(uint32_t* bits, uint32_t j0, uint32_t mask) {
-    if (!mask) return;
-    const uint32_t sh = j0 & 31u;
-    atomicOr(&bits[j0 >> 5], mask << sh);
-    if (sh) atomicOr(&bits[(j0 >> 5) + 1], mask >> (32u - sh));
-}
-
-__global__ void k_count_lower(uint32_t n, uint32_t v_begin, uint32_t v_end, const uint32_t* __restrict__ off,
-                              const uint32_t* __restrict__ adj,
-                              uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
-                              const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
-                              uint32_t* __restrict__ big, uint32_t* __restrict__ nbig, uint32_t* __restrict__ lowbits) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-    for (uint64_t v = v_begin + warp; v < v_end; v += nwarps) {
-        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
-        if (dv > kBigList) {
-            if (lane == 0) big[atomicAdd(nbig, 1u)] = (uint32_t)v;
-            continue;
-        }
-        uint32_t c = 0, tl = 0;
-        unsigned long long w = 0;
-        for (uint32_t j0 = b; j0 < e; j0 += 32) {
-            const uint32_t j = j0 + lane;
-            bool low = false;
-            if (j < e) {
-                const uint32_t u = adj[j];
-                if (u < n) {
-                    const uint32_t du = off[u + 1] - off[u];
-                    low = precedes(du, u, dv, (uint32_t)v);
-                    if (low) { ++c; w += du; }
-                    if (hot) tl += hot[u] >= hot_bits;
-                }
-            }
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
-            if (lane == 0) set_low_bits(lowbits, j0, mask);
-        }
-        c = __reduce_add_sync(0xFFFFFFFFu, c);
-        tl = __reduce_add_sync(0xFFFFFFFFu, tl);
-        for (int s = 16; s > 0; s >>= 1) w += __shfl_xor_sync(0xFFFFFFFFu, w, s);
-        if (lane == 0) {
-            cnt[v] = c;
-            work[v] = w;
-            if (hot) tail[v] = tl;
-        }
-    }
-}
-
-// CTA per long list (vertices collected by k_count_lower): the same counts with a block
-// reduction.
-__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x, unsigned long long* sh) {
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
-    __syncthreads();
-    unsigned long long t = 0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0ull;
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
-    }
-    __syncthreads();
-    return t;   // valid in thread 0
-}
-
-__global__ void k_count_lower_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
-                                  const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                                  uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
-                                  const uint32_t* __restrict__ hot, uint32_t hot_bits, uint32_t* __restrict__ tail,
-                                  uint32_t n, uint32_t* __restrict__ lowbits) {
-    __shared__ unsigned long long sh[32];
-    const uint32_t nb = *nbig;
-    for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
-        const uint32_t v = big[i];
-        const uint32_t b = off[v], e = off[v + 1], dv = e - b;
-        unsigned long long c = 0, w = 0, tl = 0;
-        for (uint32_t j0 = b + (threadIdx.x & ~31u); j0 < e; j0 += blockDim.x) {   // warp-uniform bounds
-            const uint32_t j = j0 + (threadIdx.x & 31u);
-            bool low = false;
-            if (j < e) {
-                const uint32_t u = adj[j];
-                if (u < n) {                 // ids >= n: rejected by the entry checks
-                    const uint32_t du = off[u + 1] - off[u];
-                    low = precedes(du, u, dv, v);
-                    if (low) { ++c; w += du; }
-                    if (hot) tl += hot[u] >= hot_bits;
-                }
-            }
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
-            if ((threadIdx.x & 31u) == 0) set_low_bits(lowbits, j0, mask);
-        }
-        c = block_sum_u64(c, sh);
-        w = block_sum_u64(w, sh);
-        tl = block_sum_u64(tl, sh);
-        if (threadIdx.x == 0) {
-            cnt[v] = (uint32_t)c;
-            work[v] = w;
-            if (hot) tail[v] = (uint32_t)tl;
-        }
-    }
-}
-
-// ---- input checks, entry-parallel -----------------------------------------------------------
-// starts: one bit per adjacency position, set where a non-empty list begins.
-// tile_v[k]: the vertex whose list holds entry k * kFillTile (the fill pass's tile map).
+// ---- entry-parallel tiles ---------------------------------------------------------------------
+// The adjacency is cut into tiles of kFillTile entries.  tile_v[k] is the vertex whose list
+// holds entry k * kFillTile.  A CTA working on tile k rebuilds the tile's owner map in shared
+// memory: the lists that start inside the tile belong to the vertices in (tile_v[k],
+// tile_v[k+1]]; their starts are scattered into the map and an inclusive max-scan spreads
+// each vertex over its entries.  Every pass over the adjacency below is entry-parallel, so a
+// hub list costs what any other entries cost.
 constexpr uint32_t kFillTile = 2048;
-__global__ void k_mark_starts(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ starts,
-                              uint32_t* __restrict__ tile_v) {
+constexpr int kFillThreads = 256;
+__device__ __forceinline__ uint32_t fill_slot(uint32_t i) { return i + (i >> 5); }   // bank skew
+
+__global__ void k_tile_map(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ tile_v) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t b = off[v], e = off[v + 1];
-        if (e > b) {
-            atomicOr(&starts[b >> 5], 1u << (b & 31u));
-            for (uint64_t k = (b + (uint64_t)kFillTile - 1) / kFillTile; k * kFillTile < e; ++k)
-                tile_v[k] = (uint32_t)v;
-        }
+        for (uint64_t k = (b + (uint64_t)kFillTile - 1) / kFillTile; k * kFillTile < e; ++k) tile_v[k] = (uint32_t)v;
     }
+}
+
+// Owner map of tile k (entries [t0, t0 + len)): owner[fill_slot(i)] = key of the vertex whose
+// list holds entry t0 + i, key(v) = (v << 32) | value(v), value(v) < 2^32.  *first = off of
+// the tile's first owner.  Ends with __syncthreads().
+template <typename Value>
+__device__ __forceinline__ void tile_owner_map(uint64_t k, uint64_t t0, uint32_t len, uint64_t ntiles, uint32_t n,
+                                               const uint32_t* __restrict__ off, const uint32_t* __restrict__ tile_v,
+                                               unsigned long long* owner, unsigned long long* warp_max,
+                                               uint32_t* first, Value value) {
+    constexpr int kPer = kFillTile / kFillThreads;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t v0 = tile_v[k];
+    const uint32_t v1 = k + 1 < ntiles ? tile_v[k + 1] : n - 1;   // owner of the next tile's first entry
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) owner[fill_slot(q * kFillThreads + tid)] = 0;
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t b = off[v0];
+        owner[0] = ((unsigned long long)v0 << 32) | value(v0, b, off[v0 + 1]);
+        *first = b;
+    }
+    for (uint64_t v = (uint64_t)v0 + 1 + tid; v <= v1; v += kFillThreads) {
+        const uint32_t b = off[v], e = off[v + 1];
+        if (b < t0 + len && e > b)
+            owner[fill_slot((uint32_t)(b - t0))] = (v << 32) | value((uint32_t)v, b, e);
+    }
+    __syncthreads();
+    unsigned long long x[kPer], run = 0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        run = max(run, owner[fill_slot(tid * kPer + q)]);
+        x[q] = run;
+    }
+    unsigned long long incl = run;
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+        if (lane >= (uint32_t)s) incl = max(incl, y);
+    }
+    unsigned long long pre = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+    if (lane == 0) pre = 0;
+    if (lane == 31) warp_max[wid] = incl;
+    __syncthreads();
+    for (uint32_t w = 0; w < wid; ++w) pre = max(pre, warp_max[w]);
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) owner[fill_slot(tid * kPer + q)] = max(pre, x[q]);
+    __syncthreads();
+}
+
+struct KeyDegree {
+    __device__ uint32_t operator()(uint32_t, uint32_t b, uint32_t e) const { return e - b; }
+};
+struct KeyNone {
+    __device__ uint32_t operator()(uint32_t, uint32_t, uint32_t) const { return 0; }
+};
+
+// Entries [j_begin, j_end) of whole lists (one chunk of the upload): the input checks, the
+// hot-id mapping and the orientation count in one read of the adjacency.  Per entry j of
+// the list of v: w = adj[j] must be < n, differ from v (no self loop) and, unless j starts
+// the list, exceed adj[j-1]; radj[j] = hot[w] (ids >= n: 0xFFFFFFFF) when hot is given;
+// w is a lower neighbour when precedes(deg w, w, deg v, v), recorded as a bit of lowbits.
+// Per vertex, added with one atomic per warp segment (the arrays start zeroed): cnt = the
+// lower neighbours, work = the sum of their degrees, tail = the neighbours without a hot id.
+__global__ void __launch_bounds__(kFillThreads) k_orient_tiles(
+    uint64_t j_begin, uint64_t j_end, uint32_t n, uint64_t m, const uint32_t* __restrict__ off,
+    const uint32_t* __restrict__ adj, const uint32_t* __restrict__ tile_v, const uint32_t* __restrict__ hot,
+    uint32_t hot_bits, uint32_t* __restrict__ radj, uint32_t* __restrict__ cnt, unsigned long long* __restrict__ work,
+    uint32_t* __restrict__ tail, uint32_t* __restrict__ lowbits, uint32_t* __restrict__ bad, uint32_t bad_id,
+    uint32_t bad_loop, uint32_t bad_order) {
+    constexpr int kPer = kFillTile / kFillThreads;
+    __shared__ unsigned long long owner[kFillTile + kFillTile / 32];
+    __shared__ unsigned long long warp_max[kFillThreads / 32];
+    __shared__ uint32_t first;
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    const uint64_t ntiles = (m + kFillTile - 1) / kFillTile;
+    const uint64_t k_end = (j_end + kFillTile - 1) / kFillTile;
+    uint32_t flags = 0;
+    for (uint64_t k = j_begin / kFillTile + blockIdx.x; k < k_end; k += gridDim.x) {
+        const uint64_t t0 = k * kFillTile;
+        const uint32_t len = (uint32_t)min((uint64_t)kFillTile, m - t0);
+        tile_owner_map(k, t0, len, ntiles, n, off, tile_v, owner, warp_max, &first, KeyDegree{});
+#pragma unroll 2
+        for (int q = 0; q < kPer; ++q) {
+            const uint32_t i = q * kFillThreads + tid;
+            const uint64_t j = t0 + i;
+            const unsigned long long ow = owner[fill_slot(i)];
+            const uint32_t v = (uint32_t)(ow >> 32), dv = (uint32_t)ow;
+            bool low = false;
+            uint32_t c = 0, tl = 0;
+            unsigned long long ws = 0;
+            if (j >= j_begin && j < j_end) {
+                const uint32_t w = adj[j];
+                if (w >= n) {
+                    flags |= bad_id;
+                    if (hot) radj[j] = 0xFFFFFFFFu;
+                } else {
+                    if (w == v) flags |= bad_loop;
+                    const bool start = i == 0 ? j == first : (uint32_t)(owner[fill_slot(i - 1)] >> 32) != v;
+                    if (!start && w <= adj[j - 1]) flags |= bad_order;
+                    const uint32_t du = off[w + 1] - off[w];
+                    low = precedes(du, w, dv, v);
+                    if (low) { c = 1; ws = du; }
+                    if (hot) {
+                        const uint32_t h = hot[w];
+                        radj[j] = h;
+                        tl = h >= hot_bits;
+                    }
+                }
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, low);
+            if (lane == 0 && mask) atomicOr(&lowbits[j >> 5], mask);   // lane 0's j is 32-aligned
+            // segmented sums over the warp's runs of one vertex (v is non-decreasing in lane)
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, v);
+            const int lo = __ffs(peers) - 1, hi = 31 - __clz(peers);
+#pragma unroll
+            for (int s = 1; s < 32; s <<= 1) {
+                const uint32_t yc = __shfl_up_sync(0xFFFFFFFFu, c, s), yt = __shfl_up_sync(0xFFFFFFFFu, tl, s);
+                const unsigned long long yw = __shfl_up_sync(0xFFFFFFFFu, ws, s);
+                if ((int)lane - s >= lo) { c += yc; tl += yt; ws += yw; }
+            }
+            if ((int)lane == hi && (c | tl)) {
+                if (c) {
+                    atomicAdd(&cnt[v], c);
+                    atomicAdd(&work[v], ws);
+                }
+                if (tl) atomicAdd(&tail[v], tl);
+            }
+        }
+        __syncthreads();   // the owner map is rebuilt for the next tile
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    if (flags && lane == 0) atomicOr(bad, flags);
 }
 
 // Tile of kFillTile entries per CTA iteration: write the lower neighbours (bit set in
 // lowbits) in adjacency order.  Entry j goes to wpre[j / 32] + (lower bits before j in its
 // word), wpre being the exclusive scan of the words' popcounts; in adjacency order the
-// lower entries of v are exactly lo_adj[lo_off[v], lo_off[v+1]).  The pivot of each
-// entry comes from the tile's owner map: the list starts inside the tile are scattered
-// into shared memory and an inclusive max-scan spreads each vertex over its entries.
-// Entry-parallel, so a hub list costs what any other entries cost.
-constexpr int kFillThreads = 256;
-__device__ __forceinline__ uint32_t fill_slot(uint32_t i) { return i + (i >> 5); }   // bank skew
-
+// lower entries of v are exactly lo_adj[lo_off[v], lo_off[v+1]).  The pivot of each entry
+// comes from the tile's owner map.
 __global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_t m, uint32_t E,
                                                              const uint32_t* __restrict__ off,
                                                              const uint32_t* __restrict__ adj,
@@ -162,45 +181,15 @@ __global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_
                                                              const uint32_t* __restrict__ wpre,
                                                              uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
     constexpr int kPer = kFillTile / kFillThreads;
-    __shared__ uint32_t owner[kFillTile + kFillTile / 32];
-    __shared__ uint32_t warp_max[kFillThreads / 32];
-    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    __shared__ unsigned long long owner[kFillTile + kFillTile / 32];
+    __shared__ unsigned long long warp_max[kFillThreads / 32];
+    __shared__ uint32_t first;
+    const uint32_t tid = threadIdx.x;
     const uint64_t ntiles = (m + kFillTile - 1) / kFillTile;
     for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
         const uint64_t j0 = k * kFillTile;
         const uint32_t len = (uint32_t)min((uint64_t)kFillTile, m - j0);
-        const uint32_t v0 = tile_v[k];
-        const uint32_t v1 = k + 1 < ntiles ? tile_v[k + 1] : n - 1;   // owner of the next tile's first entry
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) owner[fill_slot(q * kFillThreads + tid)] = 0;
-        __syncthreads();
-        if (tid == 0) owner[0] = v0;
-        // Every list that starts inside the tile belongs to a vertex in (v0, v1].
-        for (uint64_t v = (uint64_t)v0 + 1 + tid; v <= v1; v += kFillThreads) {
-            const uint32_t b = off[v];
-            if (b < j0 + len && off[v + 1] > b) owner[fill_slot((uint32_t)(b - j0))] = (uint32_t)v;
-        }
-        __syncthreads();
-        uint32_t x[kPer], run = 0;
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            run = max(run, owner[fill_slot(tid * kPer + q)]);
-            x[q] = run;
-        }
-        uint32_t incl = run;
-#pragma unroll
-        for (int s = 1; s < 32; s <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
-            if (lane >= (uint32_t)s) incl = max(incl, y);
-        }
-        uint32_t pre = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if (lane == 0) pre = 0;
-        if (lane == 31) warp_max[wid] = incl;
-        __syncthreads();
-        for (uint32_t w = 0; w < wid; ++w) pre = max(pre, warp_max[w]);
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) owner[fill_slot(tid * kPer + q)] = max(pre, x[q]);
-        __syncthreads();
+        tile_owner_map(k, j0, len, ntiles, n, off, tile_v, owner, warp_max, &first, KeyNone{});
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const uint32_t i = q * kFillThreads + tid;
@@ -210,31 +199,12 @@ __global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_
                 const uint32_t p = wpre[j >> 5] + __popc(word & ((1u << bit) - 1u));
                 if (((word >> bit) & 1u) && p < E) {   // p < E always: the bits are the counted entries
                     lo_adj[p] = adj[j];
-                    lo_src[p] = owner[fill_slot(i)];
+                    lo_src[p] = (uint32_t)(owner[fill_slot(i)] >> 32);
                 }
             }
         }
-        __syncthreads();   // the owner map is reset for the next tile
+        __syncthreads();   // the owner map is rebuilt for the next tile
     }
-}
-
-// Entry j of some list: its value w is < n; j is not inside w's own list (that would be a
-// self-loop); unless j starts a list, w is above the previous entry.
-// Entries [j_begin, j_end).
-__global__ void k_check_entries(uint64_t j_begin, uint64_t j_end, uint32_t n, const uint32_t* __restrict__ off,
-                                const uint32_t* __restrict__ adj, const uint32_t* __restrict__ starts,
-                                uint32_t* __restrict__ bad, uint32_t bad_id, uint32_t bad_loop, uint32_t bad_order) {
-    uint32_t flags = 0;
-    for (uint64_t j = j_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < j_end;
-         j += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t w = adj[j];
-        if (w >= n) { flags |= bad_id; continue; }
-        if (off[w] <= j && j < off[w + 1]) flags |= bad_loop;
-        const bool start = (starts[j >> 5] >> (j & 31u)) & 1u;
-        if (!start && j > 0 && w <= adj[j - 1]) flags |= bad_order;
-    }
-    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
-    if (flags && (threadIdx.x & 31) == 0) atomicOr(bad, flags);
 }
 
 // ---- hot ids for the bitmap path -----------------------------------------------------------
@@ -273,16 +243,6 @@ __global__ void k_hot_assign(uint32_t n, const uint32_t* __restrict__ off, uint3
         if (lane == 0 && mask) base = atomicAdd(counter, __popc(mask));
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (v < n) hot[v] = is_hot ? base + __popc(mask & ((1u << lane) - 1u)) : hot_bits + (uint32_t)v;
-    }
-}
-
-// Entries [j_begin, j_end); ids >= n (rejected by the entry checks) map to 0xFFFFFFFF.
-__global__ void k_map_adj(uint64_t j_begin, uint64_t j_end, uint32_t n, const uint32_t* __restrict__ adj,
-                          const uint32_t* __restrict__ hot, uint32_t* __restrict__ radj) {
-    for (uint64_t j = j_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < j_end;
-         j += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t w = adj[j];
-        radj[j] = w < n ? hot[w] : 0xFFFFFFFFu;
     }
 }
 

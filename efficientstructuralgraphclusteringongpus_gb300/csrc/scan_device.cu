@@ -368,16 +368,11 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         }
         if (mode == 2 && min_bin > 1) bitmap_path = false;   // some vertex would have a tail
     }
-    uint32_t* starts = nullptr;                                 // later: the fill pass's word prefix
-    SCAN_TRY(dalloc(d.get(), &starts, (m + 31) / 32 + 1));
     const uint64_t fill_tiles = (m + kFillTile - 1) / kFillTile;
-    uint32_t* tile_v = nullptr;
+    uint32_t* tile_v = nullptr;                                // first vertex of each adjacency tile
     SCAN_TRY(dalloc(d.get(), &tile_v, fill_tiles + 1));
-    uint32_t* big_list = nullptr;
-    SCAN_TRY(dalloc(d.get(), &big_list, m / kBigList + 2));   // at most m / kBigList long lists
     uint32_t* lowbits = nullptr;                               // one bit per entry: lower neighbour
     SCAN_TRY(dalloc(d.get(), &lowbits, m / 32 + 2));
-    uint32_t* nbig = flags + 16;
     if (bitmap_path) {
         SCAN_TRY(dalloc(d.get(), &d->hot, n));
         SCAN_TRY(dalloc(d.get(), &d->radj, m + kAdjPad));
@@ -385,9 +380,9 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     }
 
     // The adjacency arrives in chunks of whole vertex ranges; each chunk's entry checks,
-    // hot-id mapping and orientation count run on a second stream while the next chunk is
-    // copied.  The count kernels skip ids >= n, so no host check has to come in between;
-    // the flags are read once, after the count.
+    // hot-id mapping and orientation count (one pass, k_orient_tiles) run on a second stream
+    // while the next chunk is copied.  The pass skips ids >= n, so no host check has to come
+    // in between; the flags are read once, after the count.
     cudaStream_t s2 = nullptr;
     SCAN_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
     constexpr int kMaxChunks = 4;
@@ -412,13 +407,15 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
         vcut[c] = (uint32_t)lo;
     }
     scan_status ost = SCAN_OK;
+    uint32_t orient_launches = 0;
     auto enqueue = [&]() -> scan_status {
         for (auto& e : ev_chunk) SCAN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         // on s2, needing only the offsets (already on the device)
-        SCAN_CUDA(cudaMemsetAsync(starts, 0, ((m + 31) / 32 + 1) * sizeof(uint32_t), s2));
-        SCAN_CUDA(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), s2));
         SCAN_CUDA(cudaMemsetAsync(lowbits, 0, (m / 32 + 2) * sizeof(uint32_t), s2));
-        k_mark_starts<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, starts, tile_v);
+        SCAN_CUDA(cudaMemsetAsync(cnt, 0, n * sizeof(uint32_t), s2));
+        SCAN_CUDA(cudaMemsetAsync(d->work, 0, n * sizeof(unsigned long long), s2));
+        if (bitmap_path) SCAN_CUDA(cudaMemsetAsync(d->tailc, 0, n * sizeof(uint32_t), s2));
+        k_tile_map<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, tile_v);
         if (bitmap_path)
             k_hot_assign<<<grid_for(d.get(), n, 256), 256, 0, s2>>>(d->n, d->off, min_bin, kHotBits, d->hot,
                                                                   hist + kDegBins);
@@ -436,21 +433,15 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
             SCAN_CUDA(cudaEventRecord(ev_chunk[c], s));
             SCAN_CUDA(cudaStreamWaitEvent(s2, ev_chunk[c], 0));
             if (j1 > j0) {
-                k_check_entries<<<grid_for(d.get(), j1 - j0, 256), 256, 0, s2>>>(j0, j1, d->n, d->off, d->adj, starts,
-                                                                                 flags, kBadId, kBadSelfLoop, kBadOrder);
-                if (bitmap_path)
-                    k_map_adj<<<grid_for(d.get(), j1 - j0, 256), 256, 0, s2>>>(j0, j1, d->n, d->adj, d->hot, d->radj);
+                const uint64_t tiles = (j1 + kFillTile - 1) / kFillTile - j0 / kFillTile;
+                k_orient_tiles<<<grid_for(d.get(), tiles * kFillThreads, kFillThreads), kFillThreads, 0, s2>>>(
+                    j0, j1, d->n, m, d->off, d->adj, tile_v, d->hot, kHotBits, d->radj, cnt, d->work, d->tailc,
+                    lowbits, flags, kBadId, kBadSelfLoop, kBadOrder);
+                ++orient_launches;
             }
-            const uint32_t nv = vcut[c + 1] - vcut[c];
-            if (nv)
-                k_count_lower<<<grid_for(d.get(), (uint64_t)nv * 32, 256), 256, 0, s2>>>(
-                    d->n, vcut[c], vcut[c + 1], d->off, d->adj, cnt, d->work, d->hot, kHotBits, d->tailc, big_list, nbig,
-                    lowbits);
         }
         SCAN_CUDA(cudaEventRecord(d->ev[1], s));   // end of the copies
         if (bitmap_path) SCAN_CUDA(cudaMemsetAsync(d->radj + m, 0, kAdjPad * sizeof(uint32_t), s2));
-        k_count_lower_big<<<d->num_sms * 2, 1024, 0, s2>>>(big_list, nbig, d->off, d->adj, cnt, d->work, d->hot,
-                                                            kHotBits, d->tailc, d->n, lowbits);
         SCAN_CUDA(cudaEventRecord(ev_chunk[kMaxChunks], s2));
         SCAN_CUDA(cudaStreamWaitEvent(s, ev_chunk[kMaxChunks], 0));   // back to one stream
         return SCAN_OK;
@@ -474,13 +465,14 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (d->E * 2 != m) return fail(SCAN_ERR_FORMAT, "graph is not symmetric (lower entries * 2 != m)");
     SCAN_TRY(dalloc(d.get(), &d->lo_adj, d->E));
     SCAN_TRY(dalloc(d.get(), &d->lo_src, d->E));
-    if (fill_tiles) {   // word prefix of the lower bits (into the spent start marks), then the fill
+    if (fill_tiles) {   // word prefix of the lower bits, then the fill
         const uint64_t nwords = (m + 31) / 32;
-        uint32_t* wsums = nullptr;
+        uint32_t *wpre = nullptr, *wsums = nullptr;
+        SCAN_TRY(dalloc(d.get(), &wpre, nwords + 1));
         SCAN_TRY(dalloc(d.get(), &wsums, (nwords + kScanTile - 1) / kScanTile + 1));
-        SCAN_TRY(device_scan(d.get(), lowbits, nwords, starts, wsums, true));
+        SCAN_TRY(device_scan(d.get(), lowbits, nwords, wpre, wsums, true));
         k_fill_tiles<<<grid_for(d.get(), fill_tiles * kFillThreads, kFillThreads), kFillThreads, 0, s>>>(
-            d->n, m, (uint32_t)d->E, d->off, d->adj, tile_v, lowbits, starts, d->lo_adj, d->lo_src);
+            d->n, m, (uint32_t)d->E, d->off, d->adj, tile_v, lowbits, wpre, d->lo_adj, d->lo_src);
     }
     SCAN_CUDA(cudaGetLastError());
 
@@ -504,7 +496,10 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     if (st) {
         st->ms_h2d = ev_ms(d->ev[0], d->ev[1]);
         st->ms_orient = ev_ms(d->ev[1], d->ev[2]);
-        st->kernel_launches += 11 + (fill_tiles ? 4 : 0) + (off64 ? 1 : 0) + (bitmap_path ? 3 : 0);
+        // offsets check (+ conversion), tile map, orientation passes, count scan, word scan +
+        // fill, two planner passes; the bitmap path adds the degree histogram and hot ids
+        st->kernel_launches += 2 + (off64 ? 1 : 0) + (bitmap_path ? 2 : 0) + orient_launches + (n ? 3 : 0) +
+                               (fill_tiles ? 4 : 0) + 2;
     }
     *out = d.release();
     return SCAN_OK;
