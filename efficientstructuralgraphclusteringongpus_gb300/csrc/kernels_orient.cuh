@@ -36,13 +36,19 @@ __global__ void k_tile_map(uint32_t n, const uint32_t* __restrict__ off, uint32_
 }
 
 // Owner map of tile k (entries [t0, t0 + len)): owner[fill_slot(i)] = key of the vertex whose
-// list holds entry t0 + i, key(v) = (v << 32) | value(v), value(v) < 2^32.  *first = off of
-// the tile's first owner.  Ends with __syncthreads().
-template <typename Value>
+// list holds entry t0 + i.  Key = uint64: (v << 32) | degree of v; Key = uint32: v.  Keys
+// grow with v, so the max-scan spreads them.  *first = off of the tile's first owner.  Ends
+// with __syncthreads().
+template <typename Key>
+__device__ __forceinline__ Key owner_key(uint32_t v, uint32_t b, uint32_t e) {
+    if constexpr (sizeof(Key) == 8) return ((unsigned long long)v << 32) | (e - b);
+    else return v;
+}
+
+template <typename Key>
 __device__ __forceinline__ void tile_owner_map(uint64_t k, uint64_t t0, uint32_t len, uint64_t ntiles, uint32_t n,
                                                const uint32_t* __restrict__ off, const uint32_t* __restrict__ tile_v,
-                                               unsigned long long* owner, unsigned long long* warp_max,
-                                               uint32_t* first, Value value) {
+                                               Key* owner, Key* warp_max, uint32_t* first) {
     constexpr int kPer = kFillTile / kFillThreads;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t v0 = tile_v[k];
@@ -52,28 +58,28 @@ __device__ __forceinline__ void tile_owner_map(uint64_t k, uint64_t t0, uint32_t
     __syncthreads();
     if (tid == 0) {
         const uint32_t b = off[v0];
-        owner[0] = ((unsigned long long)v0 << 32) | value(v0, b, off[v0 + 1]);
+        owner[0] = owner_key<Key>(v0, b, off[v0 + 1]);
         *first = b;
     }
     for (uint64_t v = (uint64_t)v0 + 1 + tid; v <= v1; v += kFillThreads) {
         const uint32_t b = off[v], e = off[v + 1];
         if (b < t0 + len && e > b)
-            owner[fill_slot((uint32_t)(b - t0))] = (v << 32) | value((uint32_t)v, b, e);
+            owner[fill_slot((uint32_t)(b - t0))] = owner_key<Key>((uint32_t)v, b, e);
     }
     __syncthreads();
-    unsigned long long x[kPer], run = 0;
+    Key x[kPer], run = 0;
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
         run = max(run, owner[fill_slot(tid * kPer + q)]);
         x[q] = run;
     }
-    unsigned long long incl = run;
+    Key incl = run;
 #pragma unroll
     for (int s = 1; s < 32; s <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+        const Key y = __shfl_up_sync(0xFFFFFFFFu, incl, s);
         if (lane >= (uint32_t)s) incl = max(incl, y);
     }
-    unsigned long long pre = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+    Key pre = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
     if (lane == 0) pre = 0;
     if (lane == 31) warp_max[wid] = incl;
     __syncthreads();
@@ -82,13 +88,6 @@ __device__ __forceinline__ void tile_owner_map(uint64_t k, uint64_t t0, uint32_t
     for (int q = 0; q < kPer; ++q) owner[fill_slot(tid * kPer + q)] = max(pre, x[q]);
     __syncthreads();
 }
-
-struct KeyDegree {
-    __device__ uint32_t operator()(uint32_t, uint32_t b, uint32_t e) const { return e - b; }
-};
-struct KeyNone {
-    __device__ uint32_t operator()(uint32_t, uint32_t, uint32_t) const { return 0; }
-};
 
 // Entries [j_begin, j_end) of whole lists (one chunk of the upload): the input checks, the
 // hot-id mapping and the orientation count in one read of the adjacency.  Per entry j of
@@ -114,7 +113,7 @@ __global__ void __launch_bounds__(kFillThreads) k_orient_tiles(
     for (uint64_t k = j_begin / kFillTile + blockIdx.x; k < k_end; k += gridDim.x) {
         const uint64_t t0 = k * kFillTile;
         const uint32_t len = (uint32_t)min((uint64_t)kFillTile, m - t0);
-        tile_owner_map(k, t0, len, ntiles, n, off, tile_v, owner, warp_max, &first, KeyDegree{});
+        tile_owner_map(k, t0, len, ntiles, n, off, tile_v, owner, warp_max, &first);
 #pragma unroll 2
         for (int q = 0; q < kPer; ++q) {
             const uint32_t i = q * kFillThreads + tid;
@@ -181,15 +180,15 @@ __global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_
                                                              const uint32_t* __restrict__ wpre,
                                                              uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ lo_src) {
     constexpr int kPer = kFillTile / kFillThreads;
-    __shared__ unsigned long long owner[kFillTile + kFillTile / 32];
-    __shared__ unsigned long long warp_max[kFillThreads / 32];
+    __shared__ uint32_t owner[kFillTile + kFillTile / 32];
+    __shared__ uint32_t warp_max[kFillThreads / 32];
     __shared__ uint32_t first;
     const uint32_t tid = threadIdx.x;
     const uint64_t ntiles = (m + kFillTile - 1) / kFillTile;
     for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
         const uint64_t j0 = k * kFillTile;
         const uint32_t len = (uint32_t)min((uint64_t)kFillTile, m - j0);
-        tile_owner_map(k, j0, len, ntiles, n, off, tile_v, owner, warp_max, &first, KeyNone{});
+        tile_owner_map(k, j0, len, ntiles, n, off, tile_v, owner, warp_max, &first);
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const uint32_t i = q * kFillThreads + tid;
@@ -199,7 +198,7 @@ __global__ void __launch_bounds__(kFillThreads) k_fill_tiles(uint32_t n, uint64_
                 const uint32_t p = wpre[j >> 5] + __popc(word & ((1u << bit) - 1u));
                 if (((word >> bit) & 1u) && p < E) {   // p < E always: the bits are the counted entries
                     lo_adj[p] = adj[j];
-                    lo_src[p] = (uint32_t)(owner[fill_slot(i)] >> 32);
+                    lo_src[p] = owner[fill_slot(i)];
                 }
             }
         }
