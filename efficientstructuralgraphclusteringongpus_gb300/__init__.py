@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -162,6 +163,19 @@ def load_library() -> C.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+_libc = None
+
+
+def _libc_free(addr: int) -> None:
+    """free() of a result the library malloc'd (the drop-in GPUScan's int32[n])."""
+    global _libc
+    if _libc is None:
+        _libc = C.CDLL(None)
+        _libc.free.argtypes = [C.c_void_p]
+        _libc.free.restype = None
+    _libc.free(addr)
 
 
 def _check(status: int) -> None:
@@ -382,13 +396,9 @@ def GPUScan(num_edges: np.ndarray, adj: np.ndarray, eps: float, miu: int, eid=No
                                 float(eps), int(miu))
     if not p:
         raise ScanError(4, lib.scan_last_error().decode())
-    try:
-        out = np.ctypeslib.as_array(p, shape=(n,)).copy()
-    finally:
-        libc_free = C.CDLL(None).free
-        libc_free.argtypes = [C.c_void_p]
-        libc_free.restype = None
-        libc_free(C.cast(p, C.c_void_p))
+    # The array views the library's malloc'd result and frees it when collected (no copy).
+    out = np.ctypeslib.as_array(p, shape=(n,))
+    weakref.finalize(out, _libc_free, C.cast(p, C.c_void_p).value)
     return out
 
 

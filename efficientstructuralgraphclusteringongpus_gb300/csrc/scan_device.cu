@@ -385,7 +385,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     // in between; the flags are read once, after the count.
     cudaStream_t s2 = nullptr;
     SCAN_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
-    constexpr int kMaxChunks = 4;
+    constexpr int kMaxChunks = 8;
     cudaEvent_t ev_chunk[kMaxChunks + 1] = {};
     auto cleanup = [&] {
         for (auto& e : ev_chunk)

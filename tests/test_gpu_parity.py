@@ -341,7 +341,7 @@ def test_reference_kernels_admissible(scale, seed, eps, mu):
     assert oracle.check_admissible(g.offsets(), g.adjacency(), eps, mu, REF, res.label) == viol
 
 
-# ---- uploads of 16M+ entries arrive in four chunks checked and oriented as they land ----
+# ---- uploads of 16M+ entries arrive in eight chunks checked and oriented as they land ----
 def test_chunked_upload_matches_oracle():
     g = sg.Graph.rmat(20, 16, seed=12)
     assert g.m >= (16 << 20)
@@ -350,7 +350,7 @@ def test_chunked_upload_matches_oracle():
     assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
 
 
-@pytest.mark.parametrize("where", [0.1, 0.55, 0.999])
+@pytest.mark.parametrize("where", [0.1, 0.125, 0.5, 0.55, 0.999])
 @pytest.mark.parametrize("fault", ["id", "self_loop", "order"])
 def test_chunked_upload_rejects_bad_entries(where, fault):
     g = sg.Graph.rmat(20, 16, seed=12)
@@ -373,3 +373,28 @@ def test_chunked_upload_rejects_bad_entries(where, fault):
     with pytest.raises(sg.ScanError) as e:
         sg.GPUScan(off, adj, 0.5, 2)
     assert msg in str(e.value)
+
+
+# The upload passes work on tiles of 2,048 entries; at a tile's first entry "does a list
+# start here" comes from the offsets rather than the tile's owner map.
+@pytest.mark.parametrize("scale", [12, 20])           # one chunk; eight chunks
+@pytest.mark.parametrize("fault", ["self_loop", "order"])
+def test_upload_rejects_bad_entry_at_tile_start(scale, fault):
+    g = sg.Graph.rmat(scale, 16, seed=3)
+    off = g.offsets().astype(np.uint32)
+    adj = g.adjacency().astype(np.int32).copy()
+    tile = 2048
+    starts = set(off.tolist())
+    j = next(k for k in range(tile, len(adj), tile) if k not in starts)   # inside a list
+    v = int(np.searchsorted(off, j, side="right")) - 1
+    if fault == "self_loop":
+        adj[j] = v
+        msg = "self loop"
+    else:
+        adj[j - 1], adj[j] = adj[j], adj[j - 1]
+        msg = "sorted"
+    with pytest.raises(sg.ScanError) as e:
+        sg.GPUScan(off, adj, 0.5, 2)
+    assert msg in str(e.value)
+    ok = sg.GPUScan(off, g.adjacency().astype(np.int32), 0.5, 2)   # the graph without the fault
+    assert ok.shape == (g.n,)
