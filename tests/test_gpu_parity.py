@@ -186,6 +186,22 @@ def test_common_neighbors_exact(make, bitmap):
     assert st["ms_similarity"] > 0
 
 
+def test_sparse_ids_with_long_empty_runs(bitmap):
+    # 300 active vertices 997 ids apart: each 2,048-entry tile's owner map scatters its list
+    # starts across runs of ~1,000 empty lists; one active hub spans several tiles
+    rng = np.random.default_rng(17)
+    active = np.arange(300) * 997
+    edges = {(int(a), int(b)) for a, b in zip(rng.choice(active, 9000), rng.choice(active, 9000)) if a < b}
+    edges |= {(0, int(b)) for b in active[1:]}
+    g = sg.Graph.from_edges(int(active[-1]) + 5, sorted(edges))
+    assert g.m > 4 * 2048 and g.max_degree == 299
+    for eps in ("0.2", "0.5"):
+        assert_same_as_oracle(g, eps, 3, EXACT)
+        assert_same_as_oracle(g, eps, 3, REF)
+    cn, _ = g.common_neighbors()
+    assert np.array_equal(cn, oracle.common_neighbors(g.offsets(), g.adjacency()))
+
+
 def test_wheel_hub_pipeline(bitmap):
     g = wheel(20000)
     for eps in ("0.01", "0.3"):
