@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--eps", default="0.5")
     ap.add_argument("--mu", type=int, default=5)
     ap.add_argument("--predicate", default="ref-f64", choices=["ref-f64", "exact"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
