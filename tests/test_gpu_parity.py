@@ -414,3 +414,18 @@ def test_upload_rejects_bad_entry_at_tile_start(scale, fault):
     assert msg in str(e.value)
     ok = sg.GPUScan(off, g.adjacency().astype(np.int32), 0.5, 2)   # the graph without the fault
     assert ok.shape == (g.n,)
+
+
+# The generator pins again, in the GPU suite: it runs on the GPU host, whose CPU architecture
+# differs from the one the CPU suite runs on, so the bench graph is checked on both.
+def test_rmat_generator_same_on_this_host():
+    import hashlib
+    import json
+    from pathlib import Path
+    pins = json.loads((Path(__file__).parent / "golden" / "rmat_checksums.json").read_text())
+    for scale, want in pins["rmat"].items():
+        g = sg.Graph.rmat(int(scale), 16, seed=1)
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(g.offsets(), np.uint64).tobytes())
+        h.update(np.ascontiguousarray(g.adjacency(), np.uint32).tobytes())
+        assert h.hexdigest() == want["sha256"], f"R-MAT scale {scale} differs on this host"

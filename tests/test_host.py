@@ -1,6 +1,7 @@
 """CPU tests: the C-ABI library loads and exports its header, host logic (formats, checks,
 generators, reference orientation) and the oracle's pins.  No GPU is touched here."""
 import ctypes
+import json
 import re
 from fractions import Fraction
 from pathlib import Path
@@ -255,3 +256,23 @@ def test_oracle_cluster_ids_are_min_core():
     for c in np.unique(label[cores]):
         members = cores[label[cores] == c]
         assert members.min() == c
+
+
+# ---- the generators are pinned: the bench graph must be the same on every host -----------
+def _graph_sha256(g):
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(g.offsets(), np.uint64).tobytes())
+    h.update(np.ascontiguousarray(g.adjacency(), np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def test_rmat_generator_matches_pinned_checksums():
+    pins = json.loads((Path(__file__).parent / "golden" / "rmat_checksums.json").read_text())
+    for scale, want in pins["rmat"].items():
+        g = sg.Graph.rmat(int(scale), 16, seed=1)
+        assert g.m == want["m"]
+        assert _graph_sha256(g) == want["sha256"], f"R-MAT scale {scale} changed"
+    w = pins["bench_workload"]
+    g = sg.Graph.rmat(w["scale"], 16, seed=1)
+    assert (g.n, g.m, g.num_edges, g.max_degree) == (w["n"], w["m"], w["undirected_edges"], w["max_degree"])
