@@ -164,7 +164,7 @@ def byte_models(off: np.ndarray, adj: np.ndarray, eps: str) -> dict:
     (The roofline's own figure replaces 4 sum_counted du by the list words the kernels
     report reading, which also reflects the early stop.)
     full model: the same with every edge counted (the cached counts of the serving path).
-    merge model (a merge intersection per edge, as the reference does): each edge streams both lists,
+    merge model (what a merge intersection of every edge reads): each edge streams both lists,
       B = sum_e [4 (du + dv) + 16] + 4 E = 4 sum_v d_v^2 + 20 E.
     """
     deg = np.diff(off).astype(np.int64)
