@@ -276,3 +276,18 @@ def test_rmat_generator_matches_pinned_checksums():
     w = pins["bench_workload"]
     g = sg.Graph.rmat(w["scale"], 16, seed=1)
     assert (g.n, g.m, g.num_edges, g.max_degree) == (w["n"], w["m"], w["undirected_edges"], w["max_degree"])
+
+
+# ---- the CLI's argument and input errors come before any device work ----------------------
+def test_cli_rejects_bad_arguments_and_missing_graphs(tmp_path):
+    import subprocess
+
+    from efficientstructuralgraphclusteringongpus_gb300 import build
+
+    cli = str(build.CLI)
+    p = subprocess.run([cli, str(tmp_path), "0.5"], capture_output=True, text=True)
+    assert p.returncode == 1 and "<Graph folder> <eps> <miu>" in p.stderr
+    p = subprocess.run([cli, str(tmp_path), "0.5", "5", "--predicate", "fuzzy"], capture_output=True, text=True)
+    assert p.returncode == 1 and "<Graph folder>" in p.stderr
+    p = subprocess.run([cli, str(tmp_path / "absent"), "0.5", "5"], capture_output=True, text=True)
+    assert p.returncode == 2 and "load failed" in p.stderr
