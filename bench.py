@@ -9,7 +9,11 @@ cores, union-find, attach, hub/outlier) over the graph.
   e2e       the reference-facing drop-in GPUScan() (scan_gpuscan_compat) from pinned host
             CSR buffers to host labels: H2D, orientation, SCAN, D2H and device allocation
   roofline  the common-neighbour stage, HBM bound
-  cpu_baseline  the oracle (a plain OpenMP merge-intersection SCAN) on a bounded edge sample
+  cpu_baseline  the oracle (a plain OpenMP SCAN: the reference's degree prune, merge or
+            binary-search intersection, predicate, union-find, attach, hub/outlier) over the
+            whole graph, one pass on every host core
+  parity    the last timed step's labels, roles and counters against that oracle pass, and
+            the sweep point eps=0.2, mu=2 (cores, clusters, borders, hubs) against another
   sweep     eps in {0.2, 0.4, 0.6, 0.8} x mu in {2, 5, 10} on the same resident graph
   serving / batch   the serving loop and the batched small graphs (their own configs)
 
@@ -20,6 +24,12 @@ cores, union-find, attach, hub/outlier) over the graph.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has
 no exchange step); value = all ranks' edges / max-over-ranks time.
+
+--impl reference: GPUSCAN++ has no CPU implementation, so its restatement (the oracle)
+runs the same SCAN on the host cores, on the same graph made by the oracle's own generator
+(the engine library is not loaded).  The K timed steps are K disjoint edge stripes of one
+full pass; the last step adds the predicate and the clustering.  The reference's own GPU
+kernels (its cubin, its launch order) are timed on the same graph as a context field.
 """
 from __future__ import annotations
 
@@ -53,18 +63,19 @@ def parse():
     ap.add_argument("--mu", type=int, default=5)
     ap.add_argument("--predicate", default="ref-f64", choices=["ref-f64", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the oracle pass (and the parity check)")
+    ap.add_argument("--no-reference-kernels", action="store_true",
+                    help="with --impl reference: skip the reference's GPU kernels context field")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-only", action="store_true")
     ap.add_argument("--serving-graphs", type=int, default=64)
     ap.add_argument("--serving-min-scale", type=int, default=12)
-    ap.add_argument("--serving-max-scale", type=int, default=18)
+    ap.add_argument("--serving-max-scale", type=int, default=24)
     ap.add_argument("--serving-queries", type=int, default=2000)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-only", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096)
-    ap.add_argument("--batch-max-n", type=int, default=10000)
+    ap.add_argument("--batch-max-n", type=int, default=100000)
     ap.add_argument("--no-sweep", action="store_true", help="skip the eps x mu sweep on the bench graph")
     ap.add_argument("--chung-lu", action="store_true",
                     help="instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices, ~1B edges, "
@@ -73,8 +84,6 @@ def parse():
     ap.add_argument("--cl-edges", type=int, default=1_000_000_000)
     ap.add_argument("--cl-cap", type=int, default=2_000_000)
     ap.add_argument("--cl-budget-gb", type=float, default=24.0)
-    ap.add_argument("--reference-kernels", action="store_true",
-                    help="with --impl reference: time the reference's own GPU kernels (its cubin) instead")
     return ap.parse_args()
 
 
@@ -186,35 +195,40 @@ def byte_models(off: np.ndarray, adj: np.ndarray, eps: str) -> dict:
             "counted_edges": int(counted.sum())}
 
 
-def cpu_baseline(g, eps: str, mu: int, mode: int, seconds: float) -> dict:
-    """The oracle's merge intersection + predicate on a uniform edge sample, all host cores."""
+def bench_config(args, n: int, E: int, max_degree: int, world: int) -> dict:
+    """The workload, identical in both arms' lines."""
+    return {"workload": WORKLOAD, "n": n, "undirected_edges": E, "max_degree": max_degree, "eps": args.eps,
+            "mu": args.mu, "predicate": args.predicate, "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (adjacency 4*m bytes)"}
+
+
+def cpu_baseline(off, adj, eps: str, mu: int, mode: int) -> tuple[dict, tuple]:
+    """One oracle SCAN pass over the whole graph on every host core: the reference's degree
+    prune, intersection, predicate, union-find, attach and hub/outlier.  Returns the
+    cpu_baseline record and the oracle's (label, role, counts) for the parity check."""
     from oracle import oracle
 
-    off, adj = g.offsets(), g.adjacency()
-    eu, ev = oracle.orient(off, adj)
-    E = eu.size
-    rng = np.random.default_rng(1234)
-    lib = oracle.lib()
-    import ctypes as C
+    t = time.perf_counter()
+    res = oracle.scan_ex(off, adj, eps, mu, mode, prune=True)
+    dt = time.perf_counter() - t
+    E = int(off[-1]) // 2
+    return ({"value": E / dt, "unit": "similarity edges/s", "cores": os.cpu_count(), "kind": "port",
+             "sample": f"the whole graph, one pass ({E} edges, eps {eps}, mu {mu}): the reference's degree prune, "
+                       f"merge or binary-search intersection, predicate and clustering, OpenMP on "
+                       f"{os.cpu_count()} threads, {dt:.1f} s"}, res)
 
-    def run(k):
-        idx = np.sort(rng.choice(E, size=k, replace=False))
-        su, sv = np.ascontiguousarray(eu[idx]), np.ascontiguousarray(ev[idx])
-        cn = np.zeros(k, np.uint32)
-        t = time.perf_counter()
-        lib.oracle_common_neighbors(off.ctypes.data_as(C.POINTER(C.c_uint64)),
-                                    adj.ctypes.data_as(C.POINTER(C.c_uint32)), k,
-                                    su.ctypes.data_as(C.POINTER(C.c_uint32)),
-                                    sv.ctypes.data_as(C.POINTER(C.c_uint32)), cn.ctypes.data_as(C.POINTER(C.c_uint32)))
-        return time.perf_counter() - t
 
-    k = min(E, 20000)
-    dt = run(k)
-    k = int(min(E, max(k, k * seconds / max(dt, 1e-6))))
-    dt = run(k)
-    return {"value": k / dt, "unit": "similarity edges/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{k} of {E} edges drawn uniformly (seed 1234), oracle merge intersection, "
-                      f"OpenMP on {os.cpu_count()} threads, {dt:.1f} s"}
+def parity_record(res, want) -> dict:
+    """Engine result against the oracle's: labels, roles and every run counter."""
+    label, role, counts = want
+    st = res.stats
+    got = {"cores": st["num_cores"], "clusters": st["num_clusters"], "borders": st["num_borders"],
+           "hubs": st["num_hubs"], "outliers": st["num_outliers"], "similar_edges": st["num_similar_edges"],
+           "disagreements": st["pred_disagreements"], "multi_borders": st["multi_cluster_borders"]}
+    lab_eq = bool(np.array_equal(res.label, label))
+    role_eq = bool(np.array_equal(res.role, role))
+    return {"oracle_equal": lab_eq and role_eq and got == counts, "labels_equal": lab_eq, "roles_equal": role_eq,
+            "counters_equal": got == counts, "labels_differing": int((res.label != label).sum()), "oracle": counts}
 
 
 def serving_bench(args, device: int) -> dict:
@@ -325,51 +339,77 @@ def batch_bench(args, device: int) -> dict:
     return out
 
 
-def reference_arm(args) -> None:
-    """The reference path on the host cores.  GPUSCAN++ has no CPU implementation, so the
-    oracle port (its restatement) stands in: each step counts common neighbours on a fixed
-    uniform edge sample; value = sampled edges / s."""
-    import efficientstructuralgraphclusteringongpus_gb300 as sg
+def reference_arm(args, world: int) -> None:
+    """The reference path on the host cores.  GPUSCAN++ has no CPU implementation, so its
+    restatement (the oracle) stands in, on the same graph (made by the oracle's generator:
+    the engine library is not loaded) and the same eps, mu and predicate.  The K timed steps
+    are the K disjoint edge stripes of one full SCAN pass (degree prune and intersection);
+    the last one adds the predicate, union-find, attach and hub/outlier over every edge.
+    value = E / the K steps' time.  Warm-up steps count stripes of a finer split, untimed.
+    Then the reference's own GPU kernels run on the same graph (a context field)."""
     from oracle import oracle
 
-    g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
-    off, adj = g.offsets(), g.adjacency()
-    eu, ev = oracle.orient(off, adj)
-    E = eu.size
-    rng = np.random.default_rng(1234)
-    k = min(E, 200000)
-    idx = np.sort(rng.choice(E, size=k, replace=False))
-    su, sv = np.ascontiguousarray(eu[idx]), np.ascontiguousarray(ev[idx])
-    import ctypes as C
-
-    lib = oracle.lib()
-    cn = np.zeros(k, np.uint32)
-
-    def step():
-        lib.oracle_common_neighbors(off.ctypes.data_as(C.POINTER(C.c_uint64)),
-                                    adj.ctypes.data_as(C.POINTER(C.c_uint32)), k,
-                                    su.ctypes.data_as(C.POINTER(C.c_uint32)),
-                                    sv.ctypes.data_as(C.POINTER(C.c_uint32)), cn.ctypes.data_as(C.POINTER(C.c_uint32)))
-
-    for _ in range(args.warmup):
-        step()
-    t = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t
-    v = k * args.steps / dt
-    sample = f"{k} of {E} edges drawn uniformly (seed 1234) per step, oracle merge intersection, OpenMP"
-    print(json.dumps({
+    mode = 1 if args.predicate == "ref-f64" else 0
+    off, adj = oracle.rmat(args.scale, args.edge_factor, args.seed)
+    deg = np.diff(off)
+    E = int(off[-1]) // 2
+    sp = oracle.StripedPass(off, adj, args.eps, mode)
+    warm = oracle.StripedPass(off, adj, args.eps, mode)
+    for w in range(args.warmup):
+        warm.count(w, 8 * max(args.steps, args.warmup))
+    del warm
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sp.count(k, args.steps)
+    label, role, counts = sp.finish(args.mu)
+    dt = time.perf_counter() - t0
+    v = E / dt
+    line = {
         "impl": "reference", "metric": "similarity edges/s", "value": v, "unit": "similarity edges/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor, "eps": args.eps,
-                   "mu": args.mu, "sample_edges": k},
+        "config": bench_config(args, off.size - 1, E, int(deg.max()), world),
         "cpu_baseline": {"value": v, "unit": "similarity edges/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": sample},
+                         "sample": f"one full pass over all {E} edges in {args.steps} edge stripes (one per step): "
+                                   f"the reference's degree prune, merge or binary-search intersection, predicate "
+                                   f"and clustering, OpenMP on {os.cpu_count()} threads"},
         "e2e": {"value": v, "unit": "similarity edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "GPUSCAN++ has no CPU path; the oracle's restatement is timed on the host cores",
-    }))
+        "scan": counts,
+        "note": "GPUSCAN++ is GPU-only; its restatement (the oracle) is timed on the host cores",
+    }
+    if not args.no_reference_kernels:
+        line["reference_gpu_kernels"] = reference_kernels(args, off, adj, sp.cn[:E], label)
+    print(json.dumps(line))
+
+
+def reference_kernels(args, off, adj, cn, oracle_label) -> dict:
+    """GPUSCAN++'s own kernels (GPUSCAN++/GPUScan.cu compiled unmodified into a cubin) on this
+    GPU, replayed by the oracle's harness in GPUScan()'s launch order
+    (GPUSCAN++/GPUScan.cu:800-1009), on the bench graph.  kernel_ms = summed kernel time
+    (CUDA events); the harness's host-side core/other list compaction between launches is
+    outside it.  call_ms = wall time of the whole call (allocation, H2D, kernels, D2H).  The
+    host preprocessing GPUScan() expects (getEidAndEdgeList, GPUSCAN++/Graph.cpp:52-141) is
+    done once, untimed.  The output is checked against the oracle's counts."""
+    from oracle import oracle
+
+    if not oracle.reference_kernels_available():
+        return {"unavailable": "the reference's kernel cubin was not built (needs the reference sources)"}
+    E = int(off[-1]) // 2
+    mode_ok = args.predicate == "ref-f64"
+    prep = oracle.reference_gpuscan_prepare(off, adj)
+    oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)   # warm
+    ms, walls, out = [], [], None
+    for _ in range(3):
+        t = time.perf_counter()
+        out, k = oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)
+        walls.append((time.perf_counter() - t) * 1e3)
+        ms.append(k)
+    viol = oracle.check_admissible(off, adj, args.eps, args.mu, 1, out, cn=cn)
+    return {"kernel_ms": float(np.mean(ms)), "call_ms": float(np.mean(walls)),
+            "edges_per_s": E / (float(np.mean(ms)) / 1e3), "calls": 3,
+            "admissible_vs_oracle": mode_ok and viol == {"core": 0, "border": 0, "membership": 0, "hub_rule": 0},
+            "violations": viol, "labels_equal_oracle": bool(np.array_equal(out, oracle_label)),
+            "note": "reference predicate is ref-f64; a border similar to several clusters may carry any of them"}
 
 
 def sweep_bench(g, args, mode, device: int) -> list:
@@ -430,59 +470,12 @@ def chung_lu_bench(args, device: int) -> dict:
     return out
 
 
-def reference_kernels_arm(args) -> None:
-    """The reference's own GPU kernels (GPUSCAN++/GPUScan.cu compiled unmodified into a cubin)
-    on this GPU, replayed by the oracle's harness in GPUScan()'s launch order
-    (GPUSCAN++/GPUScan.cu:800-1009).  value = E / summed kernel time (CUDA events); the
-    harness's host-side core/other list compaction between launches is outside it.  The host
-    preprocessing GPUScan() expects (getEidAndEdgeList, GPUSCAN++/Graph.cpp:52-141) is done
-    once, untimed.  e2e = E / wall time of the whole call (allocation, H2D, kernels, D2H)."""
-    import efficientstructuralgraphclusteringongpus_gb300 as sg
-    from oracle import oracle
-
-    line = {"impl": "reference", "metric": "similarity edges/s", "unit": "similarity edges/s"}
-    if not oracle.reference_kernels_available():
-        line["unavailable"] = "the reference's kernel cubin was not built (needs the reference sources)"
-        print(json.dumps(line))
-        return
-    g = sg.Graph.rmat(args.scale, args.edge_factor, seed=args.seed)
-    off, adj = g.offsets(), g.adjacency()
-    E = g.num_edges
-    prep = oracle.reference_gpuscan_prepare(off, adj)
-    for _ in range(args.warmup):
-        oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)
-    ms, walls = [], []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        _, k = oracle.reference_gpuscan(off, adj, float(args.eps), args.mu, prepared=prep)
-        walls.append(time.perf_counter() - t)
-        ms.append(k)
-    mk = float(np.mean(ms))
-    v = E / (mk * 1e-3)
-    wall = float(np.mean(walls))
-    m = int(off[-1])
-    line.update({
-        "value": v, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mk,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor, "eps": args.eps,
-                   "mu": args.mu, "predicate": "reference"},
-        "kernel_ms": [round(x, 3) for x in ms],
-        "e2e": {"value": E / wall, "unit": "similarity edges/s", "ms_per_call": wall * 1e3,
-                "h2d_bytes_per_step": 4 * (off.size + 3 * m), "d2h_bytes_per_step": 4 * g.n},
-        "note": "GPUSCAN++ kernels from its cubin, on the same GPU; summed kernel time",
-    })
-    print(json.dumps(line))
-
-
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         if rank == 0:
-            if args.reference_kernels:
-                reference_kernels_arm(args)
-            else:
-                reference_arm(args)
+            reference_arm(args, world)
         return
     import torch
 
@@ -518,8 +511,10 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     stats = []
+    last_res = None
     for _ in range(args.steps):
-        stats.append(g.run(args.eps, args.mu, mode, device=local).stats)
+        last_res = g.run(args.eps, args.mu, mode, device=local)
+        stats.append(last_res.stats)
     torch.cuda.synchronize()
     dist.barrier()
     wall = time.perf_counter() - t0
@@ -536,7 +531,7 @@ def main():
     adj32 = torch.from_numpy(adj.view(np.int32)).pin_memory()
     h_off = off32.numpy().view(np.uint32)
     h_adj = adj32.numpy()
-    e2e_value, e2e_s, e2e_matches, e2e_step_ms = None, 0.0, None, []
+    e2e_value, e2e_s, e2e_matches, e2e_step_ms, e2e_cold_ms, e2e_out = None, 0.0, None, [], [], None
     if args.e2e_steps > 0:
         sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)   # warm
         dist.barrier()
@@ -549,6 +544,14 @@ def main():
         e2e_value = world * E * args.e2e_steps / e2e_s
         check = g.run(args.eps, args.mu, sg.PRED_REF_F64, device=local).label
         e2e_matches = bool(np.array_equal(out, check))
+        e2e_out = out
+        # the same call with an empty device-buffer cache: every call allocates its buffers
+        # with cudaMalloc and frees them afterwards (untimed release before each call)
+        for _ in range(3):
+            sg.release_cached_memory()
+            ts = time.perf_counter()
+            sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)
+            e2e_cold_ms.append((time.perf_counter() - ts) * 1e3)
 
     # -- roofline of the common-neighbour stage -------------------------------------------
     bm = byte_models(off, adj, args.eps)
@@ -577,9 +580,19 @@ def main():
 
     result = None
     if rank == 0:
-        cpu = None
+        cpu, parity = None, None
         if not args.no_cpu_baseline:
-            cpu = cpu_baseline(g, args.eps, args.mu, mode, args.cpu_seconds)
+            # the oracle pass is the CPU baseline and the checker of the last timed step
+            cpu, want = cpu_baseline(off, adj, args.eps, args.mu, mode)
+            parity = {"headline": dict(parity_record(last_res, want), eps=args.eps, mu=args.mu)}
+            if (args.eps, args.mu) != ("0.2", 2):
+                _, want2 = cpu_baseline(off, adj, "0.2", 2, mode)
+                parity["sweep_point"] = dict(parity_record(g.run("0.2", 2, mode, device=local), want2),
+                                             eps="0.2", mu=2)
+            if e2e_out is not None and mode == sg.PRED_REF_F64:
+                parity["drop_in_labels_equal_oracle"] = bool(np.array_equal(e2e_out, want[0]))
+            parity["oracle_equal"] = all(v["oracle_equal"] for v in parity.values() if isinstance(v, dict)) and \
+                parity.get("drop_in_labels_equal_oracle", True)
         sweep = None if args.no_sweep else sweep_bench(g, args, mode, local)
         serving = None if args.no_serving else serving_bench(args, local)
         batch = None if args.no_batch else batch_bench(args, local)
@@ -587,15 +600,17 @@ def main():
             "metric": "similarity edges/s", "value": value, "unit": "similarity edges/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": n, "undirected_edges": E, "max_degree": g.max_degree,
-                       "eps": args.eps, "mu": args.mu, "predicate": args.predicate,
-                       "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (adjacency 4*m bytes)"},
+            "config": bench_config(args, n, E, g.max_degree, world),
             "e2e": {"value": e2e_value, "unit": "similarity edges/s", "h2d_bytes_per_step": int(4 * (n + 1) + 4 * g.m),
                     "d2h_bytes_per_step": int(4 * n), "api": "GPUScan drop-in (scan_gpuscan_compat)",
                     "ms_per_step": e2e_s / max(args.e2e_steps, 1) * 1e3,
-                    "step_ms": [round(x, 3) for x in e2e_step_ms], "labels_match_resident_run": e2e_matches},
+                    "step_ms": [round(x, 3) for x in e2e_step_ms], "labels_match_resident_run": e2e_matches,
+                    "cold_cache_step_ms": [round(x, 3) for x in e2e_cold_ms],
+                    "buffers": "steps reuse the library's cache of freed device buffers (default limit 8 GiB); "
+                               "cold_cache_step_ms: the same call after the cache was emptied"},
             "roofline": roof,
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clk,
             "gpu_launches": launches,
             "sweep": sweep,

@@ -109,6 +109,8 @@ _SIGS = {
     "scan_graph_upload_streamed": (C.c_int, [_vp, C.c_int, C.c_uint64, _u64p]),
     "scan_graph_device_bytes": (C.c_uint64, [_vp]),
     "scan_release_cached_memory": (None, []),
+    "scan_set_cached_memory_limit": (None, [C.c_uint64]),
+    "scan_cached_memory_bytes": (C.c_uint64, [C.c_int]),
     "scan_gen_rmat": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_chung_lu": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_sbm": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
@@ -468,13 +470,13 @@ class Server:
         h = _vp()
         _check(load_library().scan_server_create(device, memory_budget_bytes, max_in_flight, C.byref(h)))
         self._h = h
-        self._n = []
+        self._n = {}        # graph id -> vertex count (ids come from the library: add_graph may race)
         self._keep = {}
 
     def add_graph(self, g: "Graph") -> int:
         gid = C.c_uint32(0)
         _check(load_library().scan_server_add_graph(self._h, g._h, C.byref(gid)))
-        self._n.append(g.n)
+        self._n[gid.value] = g.n
         return gid.value
 
     def submit(self, graph_id: int, eps, mu: int, predicate: int = PRED_EXACT):
@@ -553,3 +555,17 @@ def convert_edge_list(edge_list_path, out_dir) -> tuple[int, int]:
 def count_clusters(label: np.ndarray) -> int:
     lab = np.ascontiguousarray(label, dtype=np.int32)
     return int(load_library().scan_count_clusters(_ptr(lab, C.c_int32), lab.size))
+
+
+def release_cached_memory() -> None:
+    """Return every cached device buffer (of freed graphs and drop-in calls) to the driver."""
+    load_library().scan_release_cached_memory()
+
+
+def set_cached_memory_limit(nbytes: int) -> None:
+    """Cap the per-device cache of freed device buffers (0 disables it; default 8 GiB)."""
+    load_library().scan_set_cached_memory_limit(int(nbytes))
+
+
+def cached_memory_bytes(device: int = 0) -> int:
+    return int(load_library().scan_cached_memory_bytes(device))

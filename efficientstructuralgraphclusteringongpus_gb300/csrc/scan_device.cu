@@ -98,12 +98,13 @@ namespace scan {
 
 // Device-memory cache: buffers of freed resident graphs are kept per device and handed to
 // later uploads of similar size instead of cudaFree + cudaMalloc (cudaFree synchronises
-// the whole device; both cost milliseconds at GB sizes).  At most kCacheCap bytes per
-// device are kept; scan_release_cached_memory() frees them.
-constexpr size_t kCacheCap = 32ull << 30;
+// the whole device; both cost milliseconds at GB sizes).  At most g_cache_cap bytes per
+// device are kept (8 GiB unless scan_set_cached_memory_limit says otherwise; the drop-in
+// GPUScan() on R-MAT scale 22 uses about 2.6 GB); scan_release_cached_memory() frees them.
 static std::mutex g_cache_mu;
 static std::multimap<size_t, void*> g_cache[64];
 static size_t g_cache_bytes[64] = {};
+static size_t g_cache_cap = 8ull << 30;
 
 static void* cache_take(int dev, size_t bytes, size_t* actual) {
     if (dev < 0 || dev >= 64) return nullptr;
@@ -131,10 +132,34 @@ extern "C" void scan_release_cached_memory(void) {
     if (prev >= 0) cudaSetDevice(prev);
 }
 
+extern "C" void scan_set_cached_memory_limit(uint64_t bytes) {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    g_cache_cap = bytes;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    for (int dev = 0; dev < 64; ++dev) {   // free the largest blocks until each device fits
+        if (g_cache_bytes[dev] <= bytes) continue;
+        cudaSetDevice(dev);
+        while (g_cache_bytes[dev] > bytes && !g_cache[dev].empty()) {
+            auto it = std::prev(g_cache[dev].end());
+            cudaFree(it->second);
+            g_cache_bytes[dev] -= it->first;
+            g_cache[dev].erase(it);
+        }
+    }
+    if (prev >= 0) cudaSetDevice(prev);
+}
+
+extern "C" uint64_t scan_cached_memory_bytes(int device) {
+    if (device < 0 || device >= 64) return 0;
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    return g_cache_bytes[device];
+}
+
 static void cache_give(int dev, void* p, size_t bytes) {
     if (dev < 0 || dev >= 64) { cudaFree(p); return; }
     std::lock_guard<std::mutex> lock(g_cache_mu);
-    if (g_cache_bytes[dev] + bytes > kCacheCap) { cudaFree(p); return; }
+    if (g_cache_bytes[dev] + bytes > g_cache_cap) { cudaFree(p); return; }
     g_cache[dev].emplace(bytes, p);
     g_cache_bytes[dev] += bytes;
 }

@@ -142,6 +142,7 @@ struct scan_server {
     bool stop = false;
     bool mem_blocked = false;          // the queue head waits for arena space to be returned
     bool pause_admission = false;      // a graph is being added
+    bool growing = false;              // one add_graph call is reallocating the result staging
     scan_server_counters totals{};
 };
 
@@ -382,10 +383,14 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
     std::unique_lock<std::mutex> lock(s->mu);
     // Result staging must hold the largest graph.  Growing it pauses admission and waits for
     // the slots to drain, then reallocates with the lock released (no CUDA call under it).
+    // One grower at a time: a concurrent add_graph waits for the current grow step to end,
+    // then checks again whether the staging already holds its graph.
+    s->cv_done.wait(lock, [&] { return !s->growing; });
     bool grow = false;
     for (Slot& sl : s->slots) grow |= sl.n_cap < d->n;
     scan_status grow_status = SCAN_OK;
     if (grow) {
+        s->growing = true;
         s->pause_admission = true;
         s->cv_done.wait(lock, [&] {
             for (Slot& sl : s->slots)
@@ -406,6 +411,8 @@ scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t*
         }
         lock.lock();
         s->pause_admission = false;
+        s->growing = false;
+        s->cv_done.notify_all();
     }
     if (grow_status != SCAN_OK) {
         lock.unlock();

@@ -138,9 +138,16 @@ scan_status scan_graph_upload_streamed(scan_graph* g, int device, uint64_t devic
 uint64_t scan_graph_device_bytes(const scan_graph* g);
 /* Drop the device copy (the host copy stays). */
 scan_status scan_graph_release_device(scan_graph* g);
-/* Device buffers of freed graphs are cached per device (up to 32 GiB) and reused by later
- * uploads; this returns them to the driver. */
+/* Device buffers of freed graphs (and of each drop-in GPUScan() call) are kept per device,
+ * up to a limit, and reused by later uploads of similar size: cudaMalloc and cudaFree cost
+ * milliseconds at GB sizes and cudaFree synchronises the whole device.  The memory stays
+ * allocated to this process while cached.  The limit is 8 GiB per device by default.
+ * scan_release_cached_memory returns every cached buffer to the driver;
+ * scan_set_cached_memory_limit sets the limit (0 disables the cache) and frees cached buffers
+ * above it; scan_cached_memory_bytes reports what is cached on `device`. */
 void scan_release_cached_memory(void);
+void scan_set_cached_memory_limit(uint64_t bytes);
+uint64_t scan_cached_memory_bytes(int device);
 
 /* ---- generators (deterministic for a seed on every platform) ------------------------ */
 /* R-MAT: 2^scale vertices, edge_factor*2^scale sampled pairs with quadrant probabilities
@@ -256,7 +263,10 @@ typedef struct scan_server_counters {
 
 scan_status scan_server_create(int device, uint64_t memory_budget_bytes, uint32_t max_in_flight,
                                scan_server** out);
-/* Upload g and compute its common-neighbour counts; g may be freed afterwards. */
+/* Upload g and compute its common-neighbour counts; g may be freed afterwards.  Safe from
+ * several threads and while queries run: a graph larger than any before it grows the pinned
+ * result staging, which pauses admission until the running queries finish (one grow at a
+ * time). */
 scan_status scan_server_add_graph(scan_server* s, const scan_graph* g, uint32_t* graph_id);
 /* Queue a query; out_label[n] (and out_role[n], may be NULL) are written before the ticket
  * completes.  Returns at once. */

@@ -21,7 +21,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path("/root/reference/GPUSCAN++")
+# Where the reference project's sources lie (read only); SCAN_REFERENCE_ROOT overrides it.
+REFERENCE_ROOT = Path(os.environ.get("SCAN_REFERENCE_ROOT", "/root/reference"))
+REFERENCE = REFERENCE_ROOT / "GPUSCAN++"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 
@@ -30,7 +32,7 @@ HARNESS_LIB = BUILD / "libref_harness.so"
 REF_CUBIN = REF_OUT / "gpuscan_ref.cubin"
 REF_GRAPH_LIB = REF_OUT / "libref_graph.so"
 REF_CONVERT = REF_OUT / "ref_convert"
-REFERENCE_CONVERT = Path("/root/reference/csr_convert")
+REFERENCE_CONVERT = REFERENCE_ROOT / "csr_convert"
 
 
 def _run(cmd: list[str]) -> None:
@@ -50,7 +52,7 @@ def build_oracle() -> Path:
     BUILD.mkdir(exist_ok=True)
     src = HERE / "scan_oracle.c"
     if _stale(ORACLE_LIB, src, Path(__file__)):
-        _run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(ORACLE_LIB)])
+        _run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(ORACLE_LIB), "-lm"])
     return ORACLE_LIB
 
 

@@ -1,7 +1,8 @@
 """ctypes wrapper of the oracle (oracle/scan_oracle.c) and of the reference-kernel harness.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline leg.  The product package never imports this module.
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke(), bench.py's
+CPU-baseline leg and bench.py's CPU reference arm, as the checker or the CPU baseline.  The
+product package never imports this module.
 """
 from __future__ import annotations
 
@@ -40,6 +41,19 @@ def lib() -> C.CDLL:
         L.oracle_scan.restype = C.c_int
         L.oracle_scan.argtypes = [C.c_uint64, _u64p, _u32p, C.c_int, C.c_double, C.c_uint64, C.c_uint64, C.c_int,
                                   _i32p, _u8p, _u32p, _u64p]
+        L.oracle_scan_ex.restype = C.c_int
+        L.oracle_scan_ex.argtypes = [C.c_uint64, _u64p, _u32p, C.c_int, C.c_double, C.c_uint64, C.c_uint64, C.c_int,
+                                     C.c_uint, _u32p, _i32p, _u8p, _u32p, _u64p]
+        L.oracle_check_admissible_ex.restype = C.c_int
+        L.oracle_check_admissible_ex.argtypes = [C.c_uint64, _u64p, _u32p, C.c_int, C.c_double, C.c_uint64,
+                                                 C.c_uint64, C.c_int, _u32p, _i32p, _u64p]
+        L.oracle_rmat_pairs.restype = None
+        L.oracle_rmat_pairs.argtypes = [C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64, _u64p]
+        L.oracle_csr_from_pairs.restype = C.c_int64
+        L.oracle_csr_from_pairs.argtypes = [C.c_uint64, _u64p, C.c_uint64, _u64p, _u32p]
+        L.oracle_count_stripe.restype = None
+        L.oracle_count_stripe.argtypes = [_u64p, _u32p, C.c_uint64, _u32p, _u32p, C.c_uint64, C.c_uint64, C.c_double,
+                                          C.c_uint64, C.c_uint64, C.c_uint, _u32p]
         L.oracle_memberships.restype = C.c_int64
         L.oracle_memberships.argtypes = [C.c_uint64, _u64p, _u32p, C.c_int, C.c_double, C.c_uint64, C.c_uint64,
                                          C.c_int, _i32p, _i32p, C.c_uint64]
@@ -116,6 +130,71 @@ def scan(off, adj, eps: str, mu: int, mode: int):
     return label, role, dict(zip(COUNT_KEYS, map(int, counts)))
 
 
+PRUNE = 1   # oracle_scan_ex flag: the reference's degree prune (GPUSCAN++/GPUScan.cu:145) before counting
+
+
+def scan_ex(off, adj, eps: str, mu: int, mode: int, prune: bool = False, cn=None, want_cn: bool = False):
+    """oracle_scan_ex: (label, role, counts dict[, cn used]).  prune skips the edges both
+    predicates reject by degree alone (as the reference's __prep_edge does); cn (reference
+    edge order) replaces the intersections, so one count serves several (eps, mu)."""
+    off, adj = _csr(off, adj)
+    n = off.size - 1
+    e, p, q = eps_params(eps)
+    E = int(off[-1]) // 2
+    label = np.zeros(n, np.int32)
+    role = np.zeros(n, np.uint8)
+    counts = np.zeros(8, np.uint64)
+    cn_in = None if cn is None else np.ascontiguousarray(cn, dtype=np.uint32)
+    if cn_in is not None and cn_in.size != E:
+        raise ValueError(f"cn has {cn_in.size} entries, the graph {E} edges")
+    cn_out = np.zeros(max(E, 1), np.uint32) if want_cn else None
+    if lib().oracle_scan_ex(n, _p(off, C.c_uint64), _p(adj, C.c_uint32), mode, e, p, q, mu, PRUNE if prune else 0,
+                            None if cn_in is None or E == 0 else _p(cn_in, C.c_uint32), _p(label, C.c_int32),
+                            _p(role, C.c_uint8), None if cn_out is None else _p(cn_out, C.c_uint32),
+                            _p(counts, C.c_uint64)) < 0:
+        raise ValueError("oracle_scan_ex failed")
+    res = (label, role, dict(zip(COUNT_KEYS, map(int, counts))))
+    return res + (cn_out[:E],) if want_cn else res
+
+
+class StripedPass:
+    """One oracle SCAN pass split into bounded steps: count(s, k) intersects the edges
+    e = s, s + k, ... (reference edge order, degree prune on), finish() runs the predicate
+    and the clustering on the collected counts.  Steps 0..k-1 of one k cover every edge."""
+
+    def __init__(self, off, adj, eps: str, mode: int, prune: bool = True):
+        self.off, self.adj = _csr(off, adj)
+        self.eu, self.ev = orient(self.off, self.adj)
+        self.E = self.eu.size
+        self.eps, self.mode, self.flags = eps, mode, PRUNE if prune else 0
+        self.e, self.p, self.q = eps_params(eps)
+        self.cn = np.zeros(max(self.E, 1), np.uint32)
+
+    def count(self, stripe: int, nstripes: int) -> None:
+        lib().oracle_count_stripe(_p(self.off, C.c_uint64), _p(self.adj, C.c_uint32), self.E,
+                                  _p(self.eu, C.c_uint32), _p(self.ev, C.c_uint32), stripe, nstripes, self.e, self.p,
+                                  self.q, self.flags, _p(self.cn, C.c_uint32))
+
+    def finish(self, mu: int):
+        return scan_ex(self.off, self.adj, self.eps, mu, self.mode, cn=self.cn[: self.E])
+
+
+def rmat(scale: int, edge_factor: int = 16, seed: int = 1, a: float = 0.57, b: float = 0.19, c: float = 0.19):
+    """(offsets uint64[n+1], adjacency uint32[m]) of the seeded R-MAT graph, built on the
+    CPU: the same graph as the engine's Graph.rmat (both pinned by the same checksums)."""
+    n = 1 << scale
+    k = edge_factor * n
+    pairs = np.empty(k, np.uint64)
+    lib().oracle_rmat_pairs(scale, k, a, b, c, seed, _p(pairs, C.c_uint64))
+    off = np.empty(n + 1, np.uint64)
+    adj = np.empty(max(2 * k, 1), np.uint32)
+    m = lib().oracle_csr_from_pairs(n, _p(pairs, C.c_uint64), k, _p(off, C.c_uint64), _p(adj, C.c_uint32))
+    if m < 0:
+        raise MemoryError("oracle_csr_from_pairs: allocation failed")
+    del pairs
+    return off, adj[:m].copy()
+
+
 def memberships(off, adj, eps: str, mu: int, mode: int):
     off, adj = _csr(off, adj)
     n = off.size - 1
@@ -128,14 +207,18 @@ def memberships(off, adj, eps: str, mu: int, mode: int):
     return cl[:k], vx[:k]
 
 
-def check_admissible(off, adj, eps: str, mu: int, mode: int, cand) -> dict:
+def check_admissible(off, adj, eps: str, mu: int, mode: int, cand, cn=None) -> dict:
+    """Violations of a reference-style label array against the oracle (see
+    oracle_check_admissible_ex); cn (reference edge order) replaces the intersections."""
     off, adj = _csr(off, adj)
     n = off.size - 1
     e, p, q = eps_params(eps)
     c = np.ascontiguousarray(cand, dtype=np.int32)
     viol = np.zeros(4, np.uint64)
-    if lib().oracle_check_admissible(n, _p(off, C.c_uint64), _p(adj, C.c_uint32), mode, e, p, q, mu,
-                                     _p(c, C.c_int32), _p(viol, C.c_uint64)) < 0:
+    cn_in = None if cn is None else np.ascontiguousarray(cn, dtype=np.uint32)
+    if lib().oracle_check_admissible_ex(n, _p(off, C.c_uint64), _p(adj, C.c_uint32), mode, e, p, q, mu,
+                                        None if cn_in is None or cn_in.size == 0 else _p(cn_in, C.c_uint32),
+                                        _p(c, C.c_int32), _p(viol, C.c_uint64)) < 0:
         raise ValueError("oracle_check_admissible failed")
     return dict(zip(("core", "border", "membership", "hub_rule"), map(int, viol)))
 

@@ -2,8 +2,9 @@
  * scan_oracle.c -- CPU restatement of GPUSCAN++'s SCAN semantics.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA engine: only tests/,
- * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.  The product library
- * (libscan_gb300.so) never links, loads or calls it.
+ * __graft_entry__.smoke(), bench.py's CPU-baseline leg and bench.py's CPU reference arm load
+ * it, always as the checker or the CPU baseline.  The product library (libscan_gb300.so)
+ * never links, loads or calls it.
  *
  * Pinning: the reference ships no tests or golden vectors.  This restatement is pinned
  * (a) against the reference's own host orientation (GPUSCAN++/Graph.cpp:52-141, compiled
@@ -24,12 +25,14 @@
  *                 smallest id (the reference keeps the last write)  GPUSCAN++/GPUScan.cu:654-730
  *   hub/outlier   unattached vertex whose labelled neighbours carry >= 2 distinct labels
  *                 is a hub (-1), else an outlier (-2)              GPUSCAN++/GPUScan.cu:732-798
- * The intersection here is a two-pointer merge (a different method from the engine's
- * shared-memory hash probes), over OpenMP threads when available.
+ * The intersection here is a two-pointer merge, or a binary search of the shorter list in
+ * the longer one for skewed pairs (both different methods from the engine's shared-memory
+ * hash probes), over OpenMP threads when available.
  */
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -64,15 +67,32 @@ ORACLE_API int64_t oracle_orient(uint64_t n, const uint64_t* off, const uint32_t
     return (int64_t)e;
 }
 
-/* |N(u) ∩ N(v)| by a two-pointer merge of the sorted lists. */
+/* |N(u) ∩ N(v)| of two sorted lists.  Lists of similar length: a two-pointer merge.  When
+ * one list is more than 16 times longer, each entry of the shorter one is binary-searched in
+ * the longer one, as the reference's intersect does (GPUSCAN++/GPUScan.cu:174-222); the
+ * search window starts after the previous hit position, since both lists ascend. */
 static inline uint32_t merge_count(const uint64_t* off, const uint32_t* adj, uint32_t u, uint32_t v) {
     uint64_t i = off[u], ie = off[u + 1], j = off[v], je = off[v + 1];
     uint32_t c = 0;
-    while (i < ie && j < je) {
-        uint32_t a = adj[i], b = adj[j];
-        if (a < b) ++i;
-        else if (b < a) ++j;
-        else { ++c; ++i; ++j; }
+    if (ie - i > 16 * (je - j) || je - j > 16 * (ie - i)) {
+        if (ie - i > je - j) { uint64_t t = i; i = j; j = t; t = ie; ie = je; je = t; }
+        for (; i < ie && j < je; ++i) {
+            const uint32_t x = adj[i];
+            uint64_t lo = j, hi = je;
+            while (lo < hi) {
+                const uint64_t mid = lo + (hi - lo) / 2;
+                if (adj[mid] < x) lo = mid + 1; else hi = mid;
+            }
+            j = lo;
+            if (j < je && adj[j] == x) { ++c; ++j; }
+        }
+        return c;
+    }
+    while (i < ie && j < je) {          /* branch-free step: advance the smaller side (both on a hit) */
+        const uint32_t a = adj[i], b = adj[j];
+        c += a == b;
+        i += a <= b;
+        j += b <= a;
     }
     return c;
 }
@@ -111,13 +131,53 @@ static int32_t uf_root(int32_t* parent, int32_t x) {
     return x;
 }
 
+/* The reference's 'N' degree prune (GPUSCAN++/GPUScan.cu:145, in __prep_edge): with the
+ * lower endpoint's degree du, deg_u < deg_v*eps*eps marks the edge not similar before any
+ * intersection.  The exact counterpart, (du+1) q^2 < p^2 (dv+1), holds exactly when no count
+ * can pass the exact test (T <= du - 1, so (T+2)^2 <= (du+1)^2).  An edge for which both
+ * hold is rejected by both predicates whatever its count. */
+static int pruned_both(uint32_t du, uint32_t dv, double eps, uint64_t p, uint64_t q) {
+    double deg_u = (double)(du + 1u), deg_v = (double)(dv + 1u);
+    if (!(deg_u < deg_v * eps * eps)) return 0;
+    if (p > q) return 1;                                   /* eps > 1: exact never holds */
+    return (unsigned __int128)(du + 1ull) * ((unsigned __int128)q * q) <
+           (unsigned __int128)(p * p) * (dv + 1ull);
+}
+
+#define ORACLE_PRUNE 1u
+
+/* cn of the edges e = stripe, stripe + nstripes, ... (the reference edge order given by
+ * edge_u/edge_v), with the degree prune when flags & ORACLE_PRUNE (pruned edges get 0).
+ * The stripes of one nstripes together cover every edge once, so a caller can split one
+ * pass into bounded steps and finish it with oracle_scan_ex(cn_in = cn). */
+ORACLE_API void oracle_count_stripe(const uint64_t* off, const uint32_t* adj, uint64_t E, const uint32_t* edge_u,
+                                    const uint32_t* edge_v, uint64_t stripe, uint64_t nstripes, double eps,
+                                    uint64_t p, uint64_t q, unsigned flags, uint32_t* cn) {
+    if (nstripes == 0 || stripe >= nstripes || stripe >= E) return;
+    const int64_t k = (int64_t)((E - 1 - stripe) / nstripes + 1);
+    int64_t i;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (i = 0; i < k; ++i) {
+        const uint64_t e = stripe + (uint64_t)i * nstripes;
+        const uint32_t u = edge_u[e], v = edge_v[e];
+        cn[e] = (flags & ORACLE_PRUNE) && pruned_both((uint32_t)deg_of(off, u), (uint32_t)deg_of(off, v), eps, p, q)
+                    ? 0u : merge_count(off, adj, u, v);
+    }
+}
+
 /* Full SCAN.  mode 0 = exact (p/q), 1 = ref-f64 (eps).  Outputs label[n] (cluster id /
- * -1 hub / -2 outlier) and role[n] (0 outlier, 1 hub, 2 border, 3 core).  If cn_out is not
- * NULL it receives cn in the reference edge order.  counts (may be NULL) receives
+ * -1 hub / -2 outlier) and role[n] (0 outlier, 1 hub, 2 border, 3 core).
+ * flags & ORACLE_PRUNE: edges both predicates reject by degree alone (pruned_both, the
+ * reference's __prep_edge 'N' prune) are not intersected; their cn is left 0, which both
+ * predicates reject too, so labels, roles and counts are unchanged.
+ * cn_in (may be NULL): cn of every edge in the reference edge order, used instead of
+ * intersecting.  cn_out (may be NULL) receives the counts used (0 for pruned edges).
+ * counts (may be NULL) receives
  * {cores, clusters, borders, hubs, outliers, similar_edges, disagreements, multi_borders}.
  * Returns 0, or -1 on allocation failure / asymmetric input. */
-ORACLE_API int oracle_scan(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode, double eps, uint64_t p,
-                           uint64_t q, int mu, int32_t* label, uint8_t* role, uint32_t* cn_out, uint64_t* counts) {
+ORACLE_API int oracle_scan_ex(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode, double eps,
+                              uint64_t p, uint64_t q, int mu, unsigned flags, const uint32_t* cn_in, int32_t* label,
+                              uint8_t* role, uint32_t* cn_out, uint64_t* counts) {
     uint64_t E = off[n] / 2;
     uint32_t* eu = (uint32_t*)malloc(sizeof(uint32_t) * (E ? E : 1));
     uint32_t* ev = (uint32_t*)malloc(sizeof(uint32_t) * (E ? E : 1));
@@ -133,7 +193,17 @@ ORACLE_API int oracle_scan(uint64_t n, const uint64_t* off, const uint32_t* adj,
     uint64_t c_sim = 0, c_dis = 0;
     if (!eu || !ev || !cn || !sim || !sd || !parent || !bmin || !bmax || !nmin || !nmax) goto done;
     if (oracle_orient(n, off, adj, eu, ev) < 0) goto done;
-    oracle_common_neighbors(off, adj, E, eu, ev, cn);
+    if (cn_in) {
+        memcpy(cn, cn_in, sizeof(uint32_t) * E);
+    } else if (flags & ORACLE_PRUNE) {
+        int64_t i;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (i = 0; i < (int64_t)E; ++i)
+            cn[i] = pruned_both((uint32_t)deg_of(off, eu[i]), (uint32_t)deg_of(off, ev[i]), eps, p, q)
+                        ? 0u : merge_count(off, adj, eu[i], ev[i]);
+    } else {
+        oracle_common_neighbors(off, adj, E, eu, ev, cn);
+    }
     for (uint64_t e = 0; e < E; ++e) {
         uint32_t du = (uint32_t)deg_of(off, eu[e]), dv = (uint32_t)deg_of(off, ev[e]);
         int r = oracle_ref_f64_similar(cn[e], du, dv, eps);
@@ -196,6 +266,12 @@ done:
     return rc;
 }
 
+/* oracle_scan_ex with every edge intersected (no prune, no given counts). */
+ORACLE_API int oracle_scan(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode, double eps, uint64_t p,
+                           uint64_t q, int mu, int32_t* label, uint8_t* role, uint32_t* cn_out, uint64_t* counts) {
+    return oracle_scan_ex(n, off, adj, mode, eps, p, q, mu, 0u, NULL, label, role, cn_out, counts);
+}
+
 /* All (cluster, vertex) memberships: cores once, borders once per cluster they are
  * similar to, sorted by (cluster, vertex).  Returns the pair count; writes at most cap. */
 static int cmp_u64(const void* a, const void* b) {
@@ -250,9 +326,11 @@ out:
  *   [1] borders whose label is not one of their clusters
  *   [2] non-members labelled >= 0 (or members labelled < 0)
  *   [3] hub/outlier decisions that disagree with the hub rule applied to cand's own labels
+ * cn_in (may be NULL): every edge's cn in the reference edge order, instead of intersecting.
  * Returns 0, or -1 on allocation failure. */
-ORACLE_API int oracle_check_admissible(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode, double eps,
-                                       uint64_t p, uint64_t q, int mu, const int32_t* cand, uint64_t* viol) {
+ORACLE_API int oracle_check_admissible_ex(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode,
+                                          double eps, uint64_t p, uint64_t q, int mu, const uint32_t* cn_in,
+                                          const int32_t* cand, uint64_t* viol) {
     int32_t* label = (int32_t*)malloc(sizeof(int32_t) * n);
     uint8_t* role = (uint8_t*)malloc(n);
     uint64_t E = off[n] / 2;
@@ -263,7 +341,7 @@ ORACLE_API int oracle_check_admissible(uint64_t n, const uint64_t* off, const ui
     int rc = -1;
     viol[0] = viol[1] = viol[2] = viol[3] = 0;
     if (!label || !role || !cn || !eu || !ev || !ok) goto out2;
-    if (oracle_scan(n, off, adj, mode, eps, p, q, mu, label, role, cn, NULL) < 0) goto out2;
+    if (oracle_scan_ex(n, off, adj, mode, eps, p, q, mu, 0u, cn_in, label, role, cn, NULL) < 0) goto out2;
     oracle_orient(n, off, adj, eu, ev);
     /* ok[v] = 1 when cand[v] is one of v's memberships */
     for (uint64_t v = 0; v < n; ++v) if (role[v] == 3 && cand[v] == label[v]) ok[v] = 1;
@@ -298,6 +376,11 @@ ORACLE_API int oracle_check_admissible(uint64_t n, const uint64_t* off, const ui
 out2:
     free(label); free(role); free(cn); free(eu); free(ev); free(ok);
     return rc;
+}
+
+ORACLE_API int oracle_check_admissible(uint64_t n, const uint64_t* off, const uint32_t* adj, int mode, double eps,
+                                       uint64_t p, uint64_t q, int mu, const int32_t* cand, uint64_t* viol) {
+    return oracle_check_admissible_ex(n, off, adj, mode, eps, p, q, mu, NULL, cand, viol);
 }
 
 /* eid[m] for every directed entry in the reference's edge order (GPUSCAN++/Graph.cpp:95-111):
@@ -335,4 +418,98 @@ ORACLE_API int oracle_eid(uint64_t n, const uint64_t* off, const uint32_t* adj, 
 out3:
     free(hr); free(pre);
     return rc;
+}
+
+/* ---- seeded R-MAT graphs ------------------------------------------------------------------
+ * The same graphs the engine's generator (scan_gen_rmat) builds, so that the CPU reference
+ * path and the tests can make the benchmark inputs without loading the engine.  Both are
+ * pinned by the same checksums (tests/golden/rmat_checksums.json).  Pair i draws `scale`
+ * quadrant choices from its own splitmix64 stream (Steele, Lea, Flood 2014): a 64-bit draw
+ * r picks the top-left quadrant below a*2^64, top-right below (a+b)*2^64, bottom-left below
+ * (a+b+c)*2^64, else bottom-right.  The pairs are then symmetrised, self-loops dropped,
+ * each list sorted and repeats merged. */
+static inline uint64_t sm_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline uint64_t prob_threshold(double x) { return x >= 1.0 ? ~0ull : (uint64_t)ldexp(x, 63) * 2; }
+
+ORACLE_API void oracle_rmat_pairs(int scale, uint64_t num_pairs, double a, double b, double c, uint64_t seed,
+                                  uint64_t* pairs) {
+    const uint64_t ta = prob_threshold(a), tab = prob_threshold(a + b), tabc = prob_threshold(a + b + c);
+    int64_t i;
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < (int64_t)num_pairs; ++i) {
+        uint64_t s = sm_mix(seed * 0x9E3779B97F4A7C15ull + sm_mix((uint64_t)i + 0x632BE59BD9B4E019ull));
+        uint32_t u = 0, v = 0;
+        for (int l = 0; l < scale; ++l) {
+            s += 0x9E3779B97F4A7C15ull;
+            const uint64_t r = sm_mix(s);
+            u = (u << 1) | (uint32_t)(r >= tab);
+            v = (v << 1) | (uint32_t)((r >= ta && r < tab) || r >= tabc);
+        }
+        pairs[i] = ((uint64_t)u << 32) | v;
+    }
+}
+
+static int cmp_u32(const void* x, const void* y) {
+    uint32_t a = *(const uint32_t*)x, b = *(const uint32_t*)y;
+    return a < b ? -1 : a > b;
+}
+
+/* Symmetric CSR from vertex pairs (u << 32 | v): self-loops and ids >= n dropped, lists
+ * sorted ascending without repeats.  off[n+1]; adj needs room for 2*num_pairs entries.
+ * Returns m (directed entries), or -1 on allocation failure. */
+ORACLE_API int64_t oracle_csr_from_pairs(uint64_t n, const uint64_t* pairs, uint64_t num_pairs, uint64_t* off,
+                                         uint32_t* adj) {
+    uint32_t* cnt = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
+    uint64_t* cur = (uint64_t*)malloc(sizeof(uint64_t) * (n + 1));
+    uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (2 * num_pairs + 1));
+    int64_t m = -1, i;
+    if (!cnt || !cur || !tmp) goto out;
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < (int64_t)num_pairs; ++i) {
+        const uint32_t u = (uint32_t)(pairs[i] >> 32), v = (uint32_t)pairs[i];
+        if (u == v || u >= n || v >= n) continue;
+#pragma omp atomic
+        cnt[u]++;
+#pragma omp atomic
+        cnt[v]++;
+    }
+    cur[0] = 0;
+    for (uint64_t x = 0; x < n; ++x) cur[x + 1] = cur[x] + cnt[x];
+    memcpy(off, cur, sizeof(uint64_t) * (n + 1));          /* raw list starts, for now */
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < (int64_t)num_pairs; ++i) {
+        const uint32_t u = (uint32_t)(pairs[i] >> 32), v = (uint32_t)pairs[i];
+        uint64_t pu, pv;
+        if (u == v || u >= n || v >= n) continue;
+#pragma omp atomic capture
+        pu = cur[u]++;
+#pragma omp atomic capture
+        pv = cur[v]++;
+        tmp[pu] = v;
+        tmp[pv] = u;
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (i = 0; i < (int64_t)n; ++i) {                        /* sort, merge repeats; cnt = new degree */
+        uint32_t* l = tmp + off[i];
+        const uint64_t len = off[i + 1] - off[i];
+        if (len > 1) qsort(l, len, sizeof(uint32_t), cmp_u32);
+        uint64_t k = 0;
+        for (uint64_t j = 0; j < len; ++j)
+            if (k == 0 || l[j] != l[k - 1]) l[k++] = l[j];
+        cnt[i] = (uint32_t)k;
+    }
+    memcpy(cur, off, sizeof(uint64_t) * (n + 1));           /* cur = raw starts */
+    off[0] = 0;
+    for (uint64_t x = 0; x < n; ++x) off[x + 1] = off[x] + cnt[x];
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (i = 0; i < (int64_t)n; ++i) memcpy(adj + off[i], tmp + cur[i], sizeof(uint32_t) * cnt[i]);
+    m = (int64_t)off[n];
+out:
+    free(cnt); free(cur); free(tmp);
+    return m;
 }

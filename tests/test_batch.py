@@ -1,7 +1,8 @@
 """Batched SCAN (scan_batch_*): many graphs with their own (eps, mu) in one captured pass.
 
-Each graph's result must be identical to scan_run on that graph alone; the second run
-replays the captured CUDA graph with new parameters.
+Each graph's result must equal the oracle's SCAN of that graph at its own (eps, mu), and
+scan_run on that graph alone; the second run replays the captured CUDA graph with new
+parameters.
 """
 import numpy as np
 import pytest
@@ -29,19 +30,23 @@ def params(k, seed):
 
 
 @pytest.mark.parametrize("mode", [sg.PRED_EXACT, sg.PRED_REF_F64])
-def test_batch_matches_each_graph_alone(mode):
+def test_batch_matches_oracle_and_each_graph_alone(mode):
     graphs = small_sbm_batch(30, 1)
+    cns = [oracle.common_neighbors(g.offsets(), g.adjacency()) for g in graphs]
     with sg.Batch(graphs, 0, autotune=True) as b:
         for rep in range(2):      # rep 0 captures the CUDA graph, rep 1 replays it
             eps, mus = params(len(graphs), 10 + rep)
             labels, roles, st = b.run(eps, mus, mode)
             assert st["num_graphs"] == len(graphs) and st["graph_kernels"] > 0
-            cores = 0
-            for g, lab, rol, e, m in zip(graphs, labels, roles, eps, mus):
+            cores = clusters = 0
+            for i, (g, lab, rol, e, m) in enumerate(zip(graphs, labels, roles, eps, mus)):
+                ol, orole, oc = oracle.scan_ex(g.offsets(), g.adjacency(), e, m, mode, cn=cns[i])
+                assert np.array_equal(lab, ol) and np.array_equal(rol, orole), (i, e, m)
                 alone = g.run(e, m, mode)
                 assert np.array_equal(lab, alone.label) and np.array_equal(rol, alone.role)
-                cores += alone.stats["num_cores"]
-            assert st["num_cores"] == cores
+                cores += oc["cores"]
+                clusters += oc["clusters"]
+            assert st["num_cores"] == cores and st["num_clusters"] == clusters
 
 
 def test_autotuned_graph_matches_oracle():

@@ -93,3 +93,38 @@ def test_converter_rejects_garbage(tmp_path):
     with pytest.raises(sg.ScanError) as e:
         sg.convert_edge_list(tmp_path / "bad.txt", tmp_path / "o")
     assert e.value.status == 3
+
+
+def test_oracle_generator_matches_pinned_graphs():
+    """The oracle's R-MAT generator (used by the CPU reference arm, which does not load the
+    engine) builds the pinned graphs, byte for byte."""
+    import hashlib
+    import json
+    pins = json.loads((GOLDEN / "rmat_checksums.json").read_text())
+    for scale, want in pins["rmat"].items():
+        off, adj = oracle.rmat(int(scale), 16, seed=1)
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(off, np.uint64).tobytes())
+        h.update(np.ascontiguousarray(adj, np.uint32).tobytes())
+        assert adj.size == want["m"] and h.hexdigest() == want["sha256"], scale
+    for scale, seed in ((9, 3), (12, 7)):                 # and the engine's generator, other seeds
+        off, adj = oracle.rmat(scale, 8, seed=seed, a=0.45, b=0.15, c=0.15)
+        g = sg.Graph.rmat(scale, 8, a=0.45, b=0.15, c=0.15, seed=seed)
+        assert np.array_equal(off, g.offsets()) and np.array_equal(adj, g.adjacency())
+
+
+@pytest.mark.parametrize("eps,mu,mode", [("0.5", 5, 1), ("0.2", 2, 1), ("0.3", 3, 0), ("0.4", 2, 0), ("1.5", 1, 1)])
+def test_oracle_pruned_and_striped_passes_equal_full(eps, mu, mode):
+    """The degree prune (the reference's __prep_edge 'N' test) and a pass split into edge
+    stripes give the same labels, roles and counters as intersecting every edge."""
+    g = sg.Graph.rmat(13, 16, seed=4)
+    off, adj = g.offsets(), g.adjacency()
+    full = oracle.scan(off, adj, eps, mu, mode)
+    pruned = oracle.scan_ex(off, adj, eps, mu, mode, prune=True)
+    sp = oracle.StripedPass(off, adj, eps, mode)
+    for k in range(7):
+        sp.count(k, 7)
+    striped = sp.finish(mu)
+    from_cn = oracle.scan_ex(off, adj, eps, mu, mode, cn=oracle.common_neighbors(off, adj))
+    for other in (pruned, striped, from_cn):
+        assert np.array_equal(other[0], full[0]) and np.array_equal(other[1], full[1]) and other[2] == full[2]

@@ -1,14 +1,39 @@
 """Serving loop (scan_server_*): cached common-neighbour counts, continuous batching.
 
-Every served result must be identical to scan_run on the same graph and parameters, whether
-the query ran alone or mixed with others on the device.
+Every served result must equal the oracle's SCAN of that graph at the query's (eps, mu) and
+predicate, and equal scan_run on the same graph alone, whether the query ran alone or mixed
+with others on the device.  The oracle's counts are computed once per graph (reference edge
+order) and reused for every query on it.
 """
+import threading
+
 import numpy as np
 import pytest
 
 import efficientstructuralgraphclusteringongpus_gb300 as sg
+from oracle import oracle
 
 pytestmark = pytest.mark.gpu
+
+
+class OracleOf:
+    """The oracle's answers for one graph, its common-neighbour counts computed once."""
+
+    def __init__(self, g):
+        self.off, self.adj = g.offsets(), g.adjacency()
+        self.cn = oracle.common_neighbors(self.off, self.adj)
+
+    def scan(self, eps, mu, pred):
+        return oracle.scan_ex(self.off, self.adj, eps, mu, pred, cn=self.cn)
+
+
+def check_served(label, role, info, want, where):
+    ol, orole, oc = want
+    assert np.array_equal(label, ol), where
+    assert np.array_equal(role, orole), where
+    assert info["num_cores"] == oc["cores"], where
+    assert info["num_clusters"] == oc["clusters"], where
+    assert info["num_similar_edges"] == oc["similar_edges"], where
 
 
 def pool():
@@ -22,18 +47,19 @@ def random_queries(k, ngraphs, seed):
              int(rng.integers(0, 2))) for _ in range(k)]
 
 
-def test_mixed_queries_identical_to_alone():
+def test_mixed_queries_identical_to_alone_and_oracle():
     graphs = pool()
+    ref = [OracleOf(g) for g in graphs]
     with sg.Server(0, 256 << 20, 4) as srv:
         ids = [srv.add_graph(g) for g in graphs]
         qs = random_queries(200, len(graphs), 0)
         tickets = [srv.submit(ids[gi], eps, mu, pred) for gi, eps, mu, pred in qs]   # all in flight at once
         for t, (gi, eps, mu, pred) in zip(tickets, qs):
             label, role, info = srv.wait(t)
+            check_served(label, role, info, ref[gi].scan(eps, mu, pred), (gi, eps, mu, pred))
             alone = graphs[gi].run(eps, mu, pred)
             assert np.array_equal(label, alone.label), (gi, eps, mu, pred)
             assert np.array_equal(role, alone.role)
-            assert info["num_cores"] == alone.stats["num_cores"]
             assert info["latency_ms"] >= info["queue_ms"] >= 0
         c = srv.counters()
         assert c["completed"] == c["submitted"] == 200 and c["failed"] == 0 and c["pending"] == 0
@@ -41,13 +67,14 @@ def test_mixed_queries_identical_to_alone():
 
 def test_budget_for_one_query_at_a_time():
     graphs = pool()[:4]
+    ref = [OracleOf(g) for g in graphs]
     with sg.Server(0, 1 << 20, 8) as srv:            # about one scratch block of the scale-14 graph
         ids = [srv.add_graph(g) for g in graphs]
         qs = random_queries(40, len(graphs), 1)
         tickets = [srv.submit(ids[gi], eps, mu, pred) for gi, eps, mu, pred in qs]
         for t, (gi, eps, mu, pred) in zip(tickets, qs):
-            label, role, _ = srv.wait(t)
-            assert np.array_equal(label, graphs[gi].run(eps, mu, pred).label)
+            label, role, info = srv.wait(t)
+            check_served(label, role, info, ref[gi].scan(eps, mu, pred), (gi, eps, mu, pred))
 
 
 def test_query_above_budget_fails_others_served():
@@ -59,8 +86,8 @@ def test_query_above_budget_fails_others_served():
         with pytest.raises(sg.ScanError) as e:
             srv.wait(t_big)
         assert e.value.status == 5
-        label, _, _ = srv.wait(t_small)
-        assert np.array_equal(label, small.run("0.5", 3).label)
+        label, role, info = srv.wait(t_small)
+        check_served(label, role, info, OracleOf(small).scan("0.5", 3, sg.PRED_EXACT), "small")
 
 
 def test_replay_trace():
@@ -85,10 +112,13 @@ def boundary_graphs():
 
 
 def test_served_queries_at_predicate_boundaries():
-    """Served queries visit only the edges ranked similar at their eps (the ranking groups
-    edges by similarity threshold); at eps values on and around the exact and reference
-    boundaries every result must still equal scan_run."""
+    """Served queries decide each edge from its cached similarity threshold with one compare,
+    and test the edges whose threshold lies within a relative 1e-6 of eps^2 with the
+    predicate itself.  At eps values on and around the exact and reference boundaries
+    (degree-4 ring at eps 0.4, the degree-prune boundary at 0.5, the int-square wrap of the
+    twin hubs) every result must equal the oracle and scan_run."""
     graphs = boundary_graphs()
+    ref = [OracleOf(g) for g in graphs]
     eps_values = ["0", "0.1", "0.15", "0.2", "0.22", "0.4", "0.4999999", "0.5", "0.5000001", "0.7071", "0.99", "1",
                   "1.5"]
     with sg.Server(0, 512 << 20, 8) as srv:
@@ -98,8 +128,53 @@ def test_served_queries_at_predicate_boundaries():
         tickets = [srv.submit(ids[gi], e, mu, pred) for gi, e, mu, pred in qs]
         for t, (gi, e, mu, pred) in zip(tickets, qs):
             label, role, info = srv.wait(t)
+            check_served(label, role, info, ref[gi].scan(e, mu, pred), (gi, e, mu, pred))
             alone = graphs[gi].run(e, mu, pred)
             assert np.array_equal(label, alone.label), (gi, e, mu, pred)
-            assert np.array_equal(role, alone.role), (gi, e, mu, pred)
             assert info["num_similar_edges"] == alone.stats["num_similar_edges"], (gi, e, mu, pred)
-            assert info["num_clusters"] == alone.stats["num_clusters"], (gi, e, mu, pred)
+
+
+def test_concurrent_add_graph_while_serving():
+    """Two threads add graphs of increasing size (each larger one grows the pinned result
+    staging) while a third keeps queries on an existing graph in flight; every result must
+    still equal the oracle's."""
+    base = sg.Graph.rmat(10, 16, seed=21)
+    base_ref = OracleOf(base)
+    adds = [[sg.Graph.rmat(s, 8, seed=30 + s) for s in (11, 13, 15)],
+            [sg.Graph.rmat(s, 8, seed=40 + s) for s in (12, 14, 16)]]
+    errors, added = [], []
+    with sg.Server(0, 256 << 20, 4) as srv:
+        gid = srv.add_graph(base)
+        stop = threading.Event()
+
+        def adder(gs):
+            try:
+                for g in gs:
+                    added.append((srv.add_graph(g), g))
+            except Exception as e:   # reported below
+                errors.append(e)
+
+        def querier():
+            rng = np.random.default_rng(5)
+            try:
+                while not stop.is_set():
+                    eps, mu, pred = f"0.{int(rng.integers(1, 10))}", int(rng.integers(2, 8)), int(rng.integers(0, 2))
+                    label, role, info = srv.wait(srv.submit(gid, eps, mu, pred))
+                    check_served(label, role, info, base_ref.scan(eps, mu, pred), (eps, mu, pred))
+            except Exception as e:
+                errors.append(e)
+
+        qt = threading.Thread(target=querier)
+        qt.start()
+        ts = [threading.Thread(target=adder, args=(gs,)) for gs in adds]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        stop.set()
+        qt.join()
+        assert not errors, errors
+        assert len(added) == 6
+        for i, g in added:                      # every added graph is served correctly
+            label, role, info = srv.wait(srv.submit(i, "0.3", 3, sg.PRED_REF_F64))
+            check_served(label, role, info, OracleOf(g).scan("0.3", 3, sg.PRED_REF_F64), i)
