@@ -56,8 +56,9 @@ __global__ void k_predicate(uint64_t E, const uint32_t* __restrict__ lo_adj, con
 // Served queries on cached counts: each edge's similarity threshold, precomputed once per
 // graph, so the predicate is one compare per edge.  Edge e is similar at eps exactly when
 // eps^2 <= tau(e): tau_x = (t+2)^2 / ((du+1)(dv+1)) for the exact test, tau_r =
-// min((du+1)/(dv+1), t2/((du+1)(dv+1))) for the reference's doubles (t2 the int square;
-// -1 when it wraps negative: never similar).  Both are monotone in eps because IEEE
+// min((du+1)/(dv+1), max(4, t2)/((du+1)(dv+1))) for the reference's doubles: its 'N' prune,
+// then its 'Y' prune or its intersect test (t2 the int square, which can wrap negative; the
+// 'Y' threshold 4/((du+1)(dv+1)) still holds then).  Both are monotone in eps because IEEE
 // products are.  Stored as floats; an edge whose tau lies within a relative kTauBand of
 // eps^2 (float rounding is 6e-8) is decided by the predicate itself.
 constexpr double kTauBand = 1e-6;
@@ -71,7 +72,7 @@ __global__ void k_tau(uint64_t E, const uint32_t* __restrict__ lo_adj, const uin
         const double a = (double)(t + 2u);
         tau[e] = (float)(a * a / (du1 * dv1));
         const int32_t t2 = (int32_t)((t + 2u) * (t + 2u));
-        tau[E + e] = t2 < 0 ? -1.0f : (float)fmin(du1 / dv1, (double)t2 / (du1 * dv1));
+        tau[E + e] = (float)fmin(du1 / dv1, fmax(4.0, (double)t2) / (du1 * dv1));
     }
 }
 

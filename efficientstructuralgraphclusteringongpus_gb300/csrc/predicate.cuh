@@ -14,7 +14,9 @@ namespace scan {
 //   'Y' prune  eps * eps * deg_u * deg_v <= 4.0               GPUSCAN++/GPUScan.cu:156
 //   intersect  (T+2)*(T+2) < eps * eps * (du+1) * (dv+1)      GPUSCAN++/GPUScan.cu:220-221
 // with deg_x = d_x + 1 and (T+2)*(T+2) an int product (wraps past 46340).  The 'Y' prune
-// agrees with the intersect test whenever it fires ((T+2)^2 >= 4), so it is implied.
+// agrees with the intersect test whenever the square does not wrap ((T+2)^2 >= 4), but not
+// when it wraps negative (both degrees above 46339 and eps below about 4e-5): there 'Y'
+// says similar and the intersect test would say not, so it is evaluated in its own right.
 // Only IEEE multiplies and compares are used: no contraction, identical bits on any host.
 // The 'N' prune alone: true when the degrees rule the edge out whatever t is.
 __host__ __device__ __forceinline__ bool ref_f64_never(uint32_t du, uint32_t dv, double eps) {
@@ -22,8 +24,14 @@ __host__ __device__ __forceinline__ bool ref_f64_never(uint32_t du, uint32_t dv,
     return du1 < dv1 * eps * eps;
 }
 
+__host__ __device__ __forceinline__ bool ref_f64_always(uint32_t du, uint32_t dv, double eps) {
+    const double du1 = (double)(du + 1u), dv1 = (double)(dv + 1u);
+    return eps * eps * du1 * dv1 <= 4.0;
+}
+
 __host__ __device__ __forceinline__ bool ref_f64_similar(uint32_t t, uint32_t du, uint32_t dv, double eps) {
     if (ref_f64_never(du, dv, eps)) return false;
+    if (ref_f64_always(du, dv, eps)) return true;
     const int32_t t2 = (int32_t)((t + 2u) * (t + 2u));
     return !((double)t2 < eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u));
 }
@@ -69,6 +77,7 @@ __host__ __device__ inline uint32_t exact_min_count(uint32_t du, uint32_t dv, ui
 // with !((double)(a*a) < eps*eps*(du+1)*(dv+1)), the expression of ref_f64_similar.
 __host__ __device__ inline uint32_t ref_min_count(uint32_t du, uint32_t dv, double eps) {
     if (ref_f64_never(du, dv, eps)) return kNoCount;
+    if (ref_f64_always(du, dv, eps)) return 0u;
     const double thr = eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u);
     auto ok = [&](uint32_t a) { return !((double)(int32_t)(a * a) < thr); };
     const double r = sqrt(thr);

@@ -137,9 +137,12 @@ def test_twin_hubs_count_square_wrap(leaves, bitmap):
     int square wraps and ref-f64 stops calling the edge similar; exact does not."""
     edges = [(0, 1)] + [(0, 2 + i) for i in range(leaves)] + [(1, 2 + i) for i in range(leaves)]
     g = sg.Graph.from_edges(leaves + 2, edges)
-    for eps in ("0.5", "0.99", "1"):
+    # eps 0 and 0.00001: the reference's 'Y' prune (eps^2 deg_u deg_v <= 4) calls the hub-hub
+    # edge similar even where its wrapped square says not
+    for eps in ("0", "0.00001", "0.00005", "0.5", "0.99", "1"):
         assert_same_as_oracle(g, eps, 2, EXACT)
         assert_same_as_oracle(g, eps, 2, REF)
+        assert_same_as_oracle(g, eps, 1, REF)
 
 
 @pytest.mark.parametrize("knob", ["default", "tails-free"])
