@@ -111,6 +111,7 @@ _SIGS = {
     "scan_release_cached_memory": (None, []),
     "scan_set_cached_memory_limit": (None, [C.c_uint64]),
     "scan_cached_memory_bytes": (C.c_uint64, [C.c_int]),
+    "scan_set_loop_limits": (None, [C.c_int64, C.c_int32]),
     "scan_gen_rmat": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_chung_lu": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp)]),
     "scan_gen_sbm": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
@@ -569,3 +570,8 @@ def set_cached_memory_limit(nbytes: int) -> None:
 
 def cached_memory_bytes(device: int = 0) -> int:
     return int(load_library().scan_cached_memory_bytes(device))
+
+
+def set_loop_limits(union_find_iterations: int = -1, jump_rounds_cap: int = -1) -> None:
+    """Testing: shrink the bounded device loops' limits (negative restores the default)."""
+    load_library().scan_set_loop_limits(int(union_find_iterations), int(jump_rounds_cap))

@@ -46,11 +46,7 @@ struct scan_batch {
 
 namespace {
 
-uint32_t jump_index(uint32_t n) {
-    uint32_t r = 2;
-    while ((1ull << (r - 2)) < (uint64_t)n + 1 && r < (uint32_t)kMaxJumpRounds) ++r;
-    return r - 1;
-}
+uint32_t jump_index(uint32_t n) { return jump_rounds(n) - 1; }
 
 void batch_free_device(scan_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -129,4 +129,13 @@ scan_status compute_tau(DeviceGraph* d);
 // eps text + mode -> predicate parameters.
 scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mode);
 
+// Pointer-jumping rounds queued for n vertices: enough for any forest depth
+// (ceil(log2(n + 1)) + 2, at most kMaxJumpRounds), or fewer under scan_set_loop_limits.
+// Round r raises jump_flags[r] when it moved a pointer, so jump_flags[jump_rounds(n) - 1]
+// != 0 means the flatten did not converge.
+uint32_t jump_rounds(uint32_t n);
+// CAS attempts a union may take before it gives up and raises kErrUnionFindLimit
+// (1 << 20, or the value set by scan_set_loop_limits).
+uint32_t union_find_limit();
+
 }  // namespace scan

@@ -153,10 +153,10 @@ __device__ __forceinline__ int32_t uf_find(volatile int32_t* parent, int32_t x) 
 
 // Lock-free union by smaller root id: the root of a component is its smallest core id,
 // which is the reference's cluster id (GPUSCAN++/GPUScan.cu:500-523 hooks the larger
-// root under the smaller one).
-__device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b) {
+// root under the smaller one).  At most `limit` CAS attempts; false if they all lost.
+__device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b, uint32_t limit) {
     volatile int32_t* vp = parent;
-    for (int it = 0; it < (1 << 20); ++it) {
+    for (uint32_t it = 0; it < limit; ++it) {
         a = uf_find(vp, a);
         b = uf_find(vp, b);
         if (a == b) return true;
@@ -167,13 +167,13 @@ __device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b) 
 }
 
 __global__ void k_union(uint64_t E, const uint32_t* __restrict__ lo_adj, const uint32_t* __restrict__ lo_src,
-                        const uint8_t* __restrict__ sim, int32_t* parent, RunCounters* ctr) {
+                        const uint8_t* __restrict__ sim, int32_t* parent, RunCounters* ctr, uint32_t limit) {
     if (!*(volatile uint32_t*)&ctr->any_core) return;   // no core: nothing to join
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
         if (!sim[e]) continue;
         const int32_t u = (int32_t)lo_adj[e], v = (int32_t)lo_src[e];
         if (parent[u] < 0 || parent[v] < 0) continue;   // core-core only (cores never change)
-        if (!uf_union(parent, u, v)) atomicOr(&ctr->error_flags, kErrUnionFindLimit);
+        if (!uf_union(parent, u, v, limit)) atomicOr(&ctr->error_flags, kErrUnionFindLimit);
     }
 }
 

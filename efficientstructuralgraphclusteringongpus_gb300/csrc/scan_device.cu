@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -246,10 +247,17 @@ void run_scratch_bind(RunScratch* r, void* base, uint32_t n, uint64_t E) {
     r->jump_flags = reinterpret_cast<uint32_t*>(take(4 * kMaxJumpRounds));
 }
 
-static uint32_t jump_rounds(uint32_t n) {
+// Limits of the bounded device loops.  Tests shrink them (scan_set_loop_limits) to make
+// the loops give up and check that the error reaches the caller.
+static std::atomic<uint32_t> g_union_limit{1u << 20};
+static std::atomic<uint32_t> g_jump_cap{(uint32_t)kMaxJumpRounds};
+
+uint32_t union_find_limit() { return g_union_limit.load(); }
+
+uint32_t jump_rounds(uint32_t n) {
     uint32_t r = 2;
     while ((1ull << (r - 2)) < (uint64_t)n + 1 && r < (uint32_t)kMaxJumpRounds) ++r;
-    return r;
+    return std::max(1u, std::min(r, g_jump_cap.load()));
 }
 
 static int grid_for_n(int num_sms, uint64_t items, int threads, int per_sm = 8) {
@@ -659,7 +667,7 @@ scan_status launch_cluster(const DeviceGraph* d, const RunScratch& r, cudaStream
     }
     k_core_init<<<gn, T, 0, s>>>(n, r.sd, mu, vgid, bp ? bp->gmu : nullptr, r.parent, r.bmin, r.bmax, r.nmin, r.nmax,
                                  r.ctr);
-    k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr);
+    k_union<<<ge, T, 0, s>>>(E, d->lo_adj, d->lo_src, r.sim, r.parent, r.ctr, union_find_limit());
     const uint32_t rounds = jump_rounds(n);
     if (n <= kJumpBlockMax) {
         k_jump_block<<<1, 1024, 0, s>>>(n, r.parent, r.jump_flags, rounds);
@@ -951,6 +959,13 @@ scan_status scan_memberships(scan_graph* g, int device, const char* eps_decimal,
         out_vertex[i] = (int32_t)(uint32_t)keys[i];
     }
     return SCAN_OK;
+}
+
+void scan_set_loop_limits(int64_t union_find_iterations, int32_t jump_rounds_cap) {
+    g_union_limit.store(union_find_iterations < 0 ? (1u << 20)
+                                                  : (uint32_t)std::min<int64_t>(union_find_iterations, 1u << 30));
+    g_jump_cap.store(jump_rounds_cap < 0 ? (uint32_t)kMaxJumpRounds
+                                         : std::max<uint32_t>(1u, std::min<uint32_t>(jump_rounds_cap, kMaxJumpRounds)));
 }
 
 int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj, const uint32_t* num_edges, const uint32_t* eid,

@@ -167,11 +167,7 @@ size_t res_bytes(uint32_t n) { return res_role_offset(n) + n; }
 const size_t kTailFlags = pad256(sizeof(RunCounters));
 const size_t kTailBytes = kTailFlags + 4 * kMaxJumpRounds;
 
-uint32_t jump_flag_index(uint32_t n) {
-    uint32_t r = 2;
-    while ((1ull << (r - 2)) < (uint64_t)n + 1 && r < (uint32_t)kMaxJumpRounds) ++r;
-    return r - 1;
-}
+uint32_t jump_flag_index(uint32_t n) { return jump_rounds(n) - 1; }
 
 // Queue q's work on slot sl (scheduler thread, lock NOT held: CUDA calls only here).
 // Returns the number of kernels launched.

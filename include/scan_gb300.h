@@ -324,6 +324,16 @@ uint64_t scan_count_clusters(const int32_t* label, uint64_t n);
 /* Shortest decimal text that reads back as `eps` (so 0.4 -> "0.4"); buf >= 32 bytes. */
 scan_status scan_eps_to_decimal(double eps, char* buf, size_t buflen);
 
+/* ---- testing -------------------------------------------------------------------------
+ * No counterpart in the reference.  Shrinks the limits of the engine's bounded device loops
+ * so that tests can make them give up: union_find_iterations CAS attempts per union (default
+ * 1 << 20; 0 makes every core-core union fail), and at most jump_rounds_cap pointer-jumping
+ * rounds in the flatten (default enough for any depth; at least 1).  A negative value
+ * restores the default.  A run whose loop gives up returns SCAN_ERR_DEVICE (a served query
+ * completes with that status); the device stays usable.  Applies to work queued after the
+ * call, process-wide; a batch keeps the rounds it was captured with. */
+void scan_set_loop_limits(int64_t union_find_iterations, int32_t jump_rounds_cap);
+
 #ifdef __cplusplus
 }
 #endif
