@@ -71,20 +71,30 @@ __global__ void k_noalloc_flags(uint32_t n, const int32_t* __restrict__ sd, int 
         is_core[v] = sd[v] >= mu ? 1 : 0;
 }
 
-// Device address of the scratch array on the current device (looked up on the first call
-// for that device).
-scan_status scratch_for_current_device(int32_t** out) {
+// Device address of the scratch array on the current device.  Looked up with that device
+// current on the first call for it, and again on every call whose stream is not being
+// captured (the lookup allocates nothing; after a cudaDeviceReset the library's module is
+// loaded anew and the array's address can change).  A captured call uses the address found
+// last, so the first call on a device has to come before any capture.
+scan_status scratch_for_current_device(cudaStream_t s, int32_t** out) {
     int dev = -1;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess) return scan::fail(SCAN_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
     if (dev < 0 || dev >= kMaxDevices) return scan::fail(SCAN_ERR_INVALID_ARG, "device index must be < 64");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    err = cudaStreamIsCapturing(s, &cap);
+    if (err != cudaSuccess)
+        return scan::fail(SCAN_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(err));
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         int32_t* ptr = nullptr;
         err = cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_similar_degree);
         if (err != cudaSuccess || !ptr)
             return scan::fail(SCAN_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
         g_scratch[dev] = ptr;
+    } else if (!g_scratch[dev]) {
+        return scan::fail(SCAN_ERR_INVALID_ARG,
+                          "scan_cores_noalloc: make the first call on a device before any stream capture");
     }
     *out = g_scratch[dev];
     return SCAN_OK;
@@ -115,10 +125,11 @@ extern "C" scan_status scan_cores_noalloc(const uint32_t* d_offsets, uint32_t n,
     if (predicate == SCAN_PRED_EXACT && p <= q && q > (1ull << 30))
         return scan::fail(SCAN_ERR_INVALID_ARG, "exact predicate: eps needs a denominator <= 2^30");
     if (p > q) { p = 1; q = 0; }   // eps > 1: the exact test never holds
-    int32_t* sd = nullptr;
-    scan_status st = scratch_for_current_device(&sd);
-    if (st != SCAN_OK) return st;
+    cudaGetLastError();   // an earlier, unrelated launch error is not this call's
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int32_t* sd = nullptr;
+    scan_status st = scratch_for_current_device(s, &sd);
+    if (st != SCAN_OK) return st;
     const int T = 256;
     const unsigned gv = (unsigned)std::min<uint64_t>((n + T - 1) / T, 4096);
     const unsigned ge = (unsigned)std::min<uint64_t>((num_edges + T - 1) / T + 1, 8192);

@@ -302,7 +302,9 @@ void scan_server_destroy(scan_server* s);
  * before it completes.  The per-vertex scratch is a fixed array built into the library
  * (4 MiB on every GPU that loads it, held until the process exits), so n above 2^20
  * returns SCAN_ERR_TOO_LARGE.  The first call on a device looks up that array's address:
- * make it before any stream capture.  All calls share the one array and it keeps the last
+ * make it before any stream capture (a captured first call returns SCAN_ERR_INVALID_ARG).
+ * Calls on a stream that is not being captured look the address up again, so a
+ * cudaDeviceReset between calls is harmless.  All calls share the one array and it keeps the last
  * call's contents (each call clears what it needs): calls that overlap on the GPU -- other
  * streams, other host threads -- race and give wrong results, so serialise them. */
 scan_status scan_cores_noalloc(const uint32_t* d_offsets, uint32_t n, const uint32_t* d_edge_u,
