@@ -6,6 +6,9 @@
   oracle/_ref/libref_graph.so      the reference's host orientation, GPUSCAN++/Graph.cpp compiled
                                    unmodified plus a C shim (only on the machine holding the sources)
   oracle/_ref/ref_convert          the reference's converter, csr_convert/EdgeListToBinsConverter.cpp
+  oracle/_ref/gpuscan_dropin       the reference's own program, GPUSCAN++/main.cpp + Graph.cpp compiled
+                                   unmodified, linked against libscan_gb300.so instead of GPUScan.cu
+                                   (x86_64 only, like libref_graph.so; it needs a GPU to run)
 
 The two oracle/_ref outputs are built from the reference sources where they lie and only
 when those sources are present; everything they produce stays out of version control.
@@ -32,6 +35,9 @@ HARNESS_LIB = BUILD / "libref_harness.so"
 REF_CUBIN = REF_OUT / "gpuscan_ref.cubin"
 REF_GRAPH_LIB = REF_OUT / "libref_graph.so"
 REF_CONVERT = REF_OUT / "ref_convert"
+REF_DROPIN = REF_OUT / "gpuscan_dropin"
+PKG_BUILD = HERE.parent / "efficientstructuralgraphclusteringongpus_gb300" / "_build"
+INCLUDE = HERE.parent / "include"
 REFERENCE_CONVERT = REFERENCE_ROOT / "csr_convert"
 
 
@@ -84,6 +90,14 @@ def build_reference() -> bool:
         _run(["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-fopenmp", "-include", "cstdint", "-include",
               "cstring", "-include", "string", f"-I{REFERENCE}", str(REFERENCE / "Graph.cpp"),
               str(HERE / "ref_graph_shim.cpp"), "-o", str(REF_GRAPH_LIB)])
+    # The reference's GPUScan program (GPUSCAN++/main.cpp + Graph.cpp, unmodified) with the
+    # engine in place of GPUScan.cu: the link-level drop-in of the makefile in INTEGRATION.md.
+    lib = PKG_BUILD / "libscan_gb300.so"
+    if platform.machine() == "x86_64" and lib.exists() and _stale(
+            REF_DROPIN, REFERENCE / "main.cpp", REFERENCE / "Graph.cpp", lib, Path(__file__)):
+        _run(["g++", "-O2", "-std=c++14", "-fopenmp", "-include", "cstdint", "-include", "cstring", "-include",
+              "string", f"-I{REFERENCE}", str(REFERENCE / "main.cpp"), str(REFERENCE / "Graph.cpp"), "-o",
+              str(REF_DROPIN), f"-L{PKG_BUILD}", "-lscan_gb300", f"-Wl,-rpath,{PKG_BUILD}"])
     # The reference's edge-list converter, unmodified (plain C++).
     if (REFERENCE_CONVERT / "EdgeListToBinsConverter.cpp").exists() and _stale(
             REF_CONVERT, REFERENCE_CONVERT / "EdgeListToBinsConverter.cpp", Path(__file__)):
