@@ -479,6 +479,133 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
     fused_totals(fp, lane, nsim, ndis);
 }
 
+// One-shot runs on the hash classes (no split pivot, predicate fused): nearly every counted
+// edge ends not similar, so an upper bound on its count decides it.  The pivot's list is
+// staged twice in shared memory: as a hashed bitmap of 2^log2bits bits (at least 32 bits
+// per entry, so a probe of a non-neighbour finds its bit set with probability <= 1/32) and
+// as a sorted copy.  Streaming a lower list counts the entries whose bit is set; every
+// common neighbour's bit is set, so the bit count B over the examined prefix plus the
+// unexamined entries bounds cn, and the early stop (needed_entries) runs on B.  A list
+// decided that way stores B < tlo, which both predicates reject like the true count.  Lists
+// whose bound reaches tlo (or with tlo = 0: any count may be similar) are recounted exactly,
+// one at a time by the whole warp, each entry binary-searched in the sorted copy.
+// A probe is one 4-byte shared load of a random word, against one 16-byte bucket load for
+// the bucketed table of k_cn_big.
+__device__ __forceinline__ uint32_t filter_bit(uint32_t w, uint32_t log2bits) {
+    return (w * 0x9E3779B1u) >> (32u - log2bits);
+}
+
+__device__ __forceinline__ uint32_t filter_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
+                                                      const uint32_t* bits, uint32_t log2bits) {
+    const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+    uint32_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t h = filter_bit(w[i], log2bits);
+        const uint32_t b = (bits[h >> 5] >> (h & 31u)) & 1u;
+        c += (p + i >= lb && p + i < le) ? b : 0u;
+    }
+    return c;
+}
+
+// |adj[b, e) ∩ list[0, dv)|, list sorted ascending: warp-wide, the result in every lane.
+__device__ __forceinline__ uint32_t sorted_count(const uint32_t* list, uint32_t dv, const uint32_t* __restrict__ adj,
+                                                 uint32_t b, uint32_t e, uint32_t lane) {
+    uint32_t c = 0;
+    for (uint32_t j = b + lane; j < e; j += 32) {
+        const uint32_t w = __ldg(adj + j);
+        uint32_t lo = 0, hi = dv;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (list[mid] < w) lo = mid + 1; else hi = mid;
+        }
+        c += (lo < dv && list[lo] == w) ? 1u : 0u;
+    }
+    return __reduce_add_sync(0xFFFFFFFFu, c);
+}
+
+// Shared memory of k_cn_filter for a class of up to `entries` pivot entries.
+__host__ __device__ constexpr uint32_t filter_log2bits(uint32_t entries) {
+    uint32_t l = 10;
+    while ((1u << l) < 32u * entries) ++l;
+    return l;
+}
+__host__ __device__ constexpr size_t filter_smem_bytes(uint32_t entries) {
+    return (size_t(1) << filter_log2bits(entries)) / 8 + size_t(entries) * 4;
+}
+
+__global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t max_entries, uint32_t* queue,
+                            const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
+                            const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
+                            CnPrune pr, unsigned long long* __restrict__ ctr, FusedPred fp) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    const uint32_t log2bits = filter_log2bits(max_entries);
+    const uint32_t nwords = (1u << log2bits) >> 5;
+    uint32_t* bits = smem;
+    uint32_t* list = smem + nwords;
+    __shared__ uint32_t next_batch, task_slot;
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long nsim = 0, ndis = 0;
+    for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
+         t = next_task(queue, t, false, &task_slot)) {
+        const CnTask tk = tasks[t];
+        const uint32_t vb = off[tk.v], ve = off[tk.v + 1], dv = ve - vb;   // dv <= max_entries (no split)
+        for (uint32_t i = threadIdx.x; i < nwords / 4; i += blockDim.x)
+            reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
+        if (threadIdx.x == 0) next_batch = 0;
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < dv; j += blockDim.x) {
+            const uint32_t w = adj[vb + j];
+            list[j] = w;
+            const uint32_t h = filter_bit(w, log2bits);
+            atomicOr(&bits[h >> 5], 1u << (h & 31u));
+        }
+        __syncthreads();
+        for (;;) {
+            uint32_t bidx = 0;
+            if (lane == 0) bidx = atomicAdd(&next_batch, 1u);
+            const uint32_t kb = tk.e0 + 32u * __shfl_sync(0xFFFFFFFFu, bidx, 0);
+            if (kb >= tk.e1) break;
+            const uint32_t k = kb + lane;
+            const bool valid = k < tk.e1;
+            uint32_t ub = 0, ue = 0, u = 0, du = 0, tlo = 0;
+            if (valid) {
+                u = lo_adj[k];
+                ub = off[u];
+                ue = off[u + 1];
+                du = ue - ub;
+                if (cn_pruned(du, dv, pr)) ue = ub;
+                if (ue > ub) tlo = min_similar_count(du, dv, pr);
+            }
+            // tlo = 0: any count may be similar, so the bound decides nothing; count exactly
+            const bool bound_scan = ue > ub && tlo > 0;
+            uint32_t words = 0;
+            uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, bound_scan ? ue : ub, tlo, long_words, words,
+                                                       [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
+                                                           return filter_probe_word(x, p, lb, le, bits, log2bits);
+                                                       });
+            uint32_t exact = __ballot_sync(0xFFFFFFFFu, ue > ub && cnt >= tlo);
+            while (exact) {
+                const int j = __ffs(exact) - 1;
+                exact &= exact - 1;
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, ub, j), e = __shfl_sync(0xFFFFFFFFu, ue, j);
+                words += ((e + 3u) >> 2) - (b >> 2);
+                const uint32_t c = sorted_count(list, dv, adj, b, e, lane);
+                if ((int)lane == j) cnt = c;
+            }
+            const uint32_t nc = __popc(__ballot_sync(0xFFFFFFFFu, ue > ub));
+            if (lane == 0 && (words | nc)) {
+                atomicAdd(&ctr[0], (unsigned long long)words);
+                atomicAdd(&ctr[1], (unsigned long long)nc);
+            }
+            if (valid) cn[k] = cnt;
+            fused_predicate(fp, pr, valid, k, u, tk.v, du, dv, cnt, lane, nsim, ndis);
+        }
+        __syncthreads();
+    }
+    fused_totals(fp, lane, nsim, ndis);
+}
+
 // Bitmap path: one CTA of kBitmapThreads per task (pivot, edge slice), one CTA per SM.
 // Shared memory: the hot bitmap (zeroed once; each task sets its pivot's bits and clears
 // them again) and the tail table.  Probing an entry is one 4-byte shared load for hot ids.

@@ -540,8 +540,11 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 
 static bool g_attr_set[64] = {};
 static bool g_attr_bitmap[64] = {};
+static bool g_attr_filter[64] = {};
 static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class (found once per device,
                                                 // so capturing launch_cn into a graph queries nothing)
+static int g_per_sm_filter[64][kNumBigClasses][2] = {};   // k_cn_filter, [class][largest class 2 at the
+                                                          // default chunk, or at the autotuner's cap]
 
 // cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
 scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune, const RunScratch* fused) {
@@ -567,20 +570,43 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
                                        (int)(big_class_slots(kNumBigClasses - 1) * sizeof(uint32_t))));
         g_attr_set[d->device] = true;
     }
+    // One-shot fused runs (every pivot unsplit) decide most edges from an upper bound on
+    // their count (k_cn_filter); full counts and split plans use the bucketed table.
+    const bool filter = fp.sim != nullptr;
+    if (filter && !g_attr_filter[d->device]) {
+        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)filter_smem_bytes(kChunkMaxCap)));
+        g_attr_filter[d->device] = true;
+    }
     for (int c = 0; c < kNumBigClasses; ++c) {
         if (d->nbig[c]) {
             const int threads = c == 0 ? 128 : 512;   // class 0: many small pivots, measured fastest
-            const size_t smem = big_class_slots(c) * sizeof(uint32_t);
-            int& per_sm = g_per_sm[d->device][c];
-            if (per_sm == 0) {
-                SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
-                per_sm = std::max(per_sm, 1);
+            if (filter) {
+                // unsplit: class 2 pivots hold up to the plan's chunk size
+                const uint32_t entries = c == kNumBigClasses - 1 ? d->plan.chunk_max : big_class_entries(c);
+                const size_t smem = filter_smem_bytes(entries);
+                int& per_sm = g_per_sm_filter[d->device][c][entries > kChunkMax ? 1 : 0];
+                if (per_sm == 0) {
+                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
+                    per_sm = std::max(per_sm, 1);
+                }
+                const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
+                k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], entries, d->task_queue + c,
+                                                                  d->off, d->adj, d->lo_adj, d->cn, d->long_words,
+                                                                  pr, d->cn_ctr, fp);
+            } else {
+                const size_t smem = big_class_slots(c) * sizeof(uint32_t);
+                int& per_sm = g_per_sm[d->device][c];
+                if (per_sm == 0) {
+                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_big, threads, smem));
+                    per_sm = std::max(per_sm, 1);
+                }
+                const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
+                k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
+                                                                d->task_queue + c, d->off,
+                                                                d->adj, d->lo_adj, d->cn, d->long_words, pr,
+                                                                d->cn_ctr, fp);
             }
-            const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-            k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
-                                                            d->task_queue + c, d->off,
-                                                            d->adj, d->lo_adj, d->cn, d->long_words, pr,
-                                                            d->cn_ctr, fp);
             ++*launches;
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
