@@ -39,6 +39,10 @@ constexpr uint32_t kTailMax = kTailSlots / 2;
 // SM: a bitmap task of a mid-size pivot leaves most of its 32 warps waiting at the task
 // barrier (R-MAT s22, eps 0.5: 33.0 ms against 38.3 ms with the threshold at 1024).
 constexpr uint32_t kBitmapMinDeg = kChunkMax;
+// Hubs up to kHubFilterMax entries (the "mid hubs") get their own task list: one-shot runs
+// count them with k_cn_filter (a 2^19-bit filter, <= 1/42 false positives, plus the sorted
+// copy: 112 KB, two CTAs per SM), full counts with k_cn_bitmap like the larger hubs.
+constexpr uint32_t kHubFilterMax = kChunkMaxCap;
 constexpr int kBitmapThreads = 1024;
 __host__ __device__ constexpr uint32_t big_class_entries(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : kChunkMax; }
 __host__ __device__ constexpr uint32_t big_class_slots(int c) { return 4u * big_class_entries(c); }   // load <= 1/4
@@ -700,8 +704,9 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
 }
 
 // Task planner.  Pass 1 (outputs null) counts tasks per class; pass 2 writes them.
-// counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks,
-// counts[5] (pass 1 only) pivots split into chunks.
+// counts[0] small pivots, counts[1 + c] tasks of hash class c, counts[4] bitmap tasks of
+// hubs above kHubFilterMax, counts[5] bitmap tasks of the mid hubs, counts[6] (pass 1 only)
+// pivots split into chunks.
 // tail (may be null: bitmap path off) holds each vertex's count of non-hot neighbours.
 // (PlanParams: device_graph.h.)
 
@@ -709,10 +714,11 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                        const unsigned long long* __restrict__ work, const uint32_t* __restrict__ tail,
                        PlanParams pp, uint32_t* __restrict__ counts, uint32_t* __restrict__ small_out,
                        CnTask* __restrict__ big0, CnTask* __restrict__ big1, CnTask* __restrict__ big2,
-                       CnTask* __restrict__ bmp) {
-    __shared__ uint32_t blk[2 + kNumBigClasses];
-    __shared__ uint32_t base[2 + kNumBigClasses];
-    if (threadIdx.x < 2 + kNumBigClasses) blk[threadIdx.x] = 0;
+                       CnTask* __restrict__ bmp, CnTask* __restrict__ hmid) {
+    constexpr int kClasses = 3 + kNumBigClasses;   // small, hash classes, big hubs, mid hubs
+    __shared__ uint32_t blk[kClasses];
+    __shared__ uint32_t base[kClasses];
+    if (threadIdx.x < kClasses) blk[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     int cls = -1;
@@ -725,7 +731,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                 cls = 0;
                 ntask = 1;
             } else if (tail && dv > kBitmapMinDeg && tail[v] <= kTailMax) {
-                cls = 1 + kNumBigClasses;
+                cls = dv <= kHubFilterMax ? 2 + kNumBigClasses : 1 + kNumBigClasses;
                 nch = 1;
                 unsigned long long s = (work[v] + pp.target_probes_bitmap - 1) / pp.target_probes_bitmap;
                 const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
@@ -740,14 +746,14 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                 const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
                 nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
                 ntask = nch * nsl;
-                if (nch > 1 && small_out == nullptr) atomicAdd(&counts[2 + kNumBigClasses], 1u);   // split pivots
+                if (nch > 1 && small_out == nullptr) atomicAdd(&counts[kClasses], 1u);   // split pivots
             }
         }
     }
     uint32_t mine = 0;
     if (cls >= 0) mine = atomicAdd(&blk[cls], ntask);
     __syncthreads();
-    if (threadIdx.x < 2 + kNumBigClasses) base[threadIdx.x] = atomicAdd(&counts[threadIdx.x], blk[threadIdx.x]);
+    if (threadIdx.x < kClasses) base[threadIdx.x] = atomicAdd(&counts[threadIdx.x], blk[threadIdx.x]);
     __syncthreads();
     if (cls < 0 || (small_out == nullptr)) return;
     const uint32_t pos = base[cls] + mine;
@@ -755,7 +761,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
         small_out[pos] = v;
         return;
     }
-    CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : cls == 3 ? big2 : bmp;
+    CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : cls == 3 ? big2 : cls == 4 ? bmp : hmid;
     const uint32_t vb = off[v], e0 = lo_off[v];
     uint32_t i = 0;
     for (uint32_t c = 0; c < nch; ++c) {
@@ -764,7 +770,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
         for (uint32_t s = 0; s < nsl; ++s, ++i) {
             CnTask t;
             t.v = v;
-            t.cb = cls == 1 + kNumBigClasses ? tail[v] : cb;
+            t.cb = cls >= 1 + kNumBigClasses ? tail[v] : cb;
             t.ce = cend;
             t.e0 = e0 + (uint32_t)((uint64_t)L * s / nsl);
             t.e1 = e0 + (uint32_t)((uint64_t)L * (s + 1) / nsl);

@@ -293,10 +293,10 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
     cudaStream_t s = d->stream;
     uint32_t* counts = d->dflags + 1;
     const unsigned pg = (unsigned)((d->n + 255) / 256);
-    SCAN_CUDA(cudaMemsetAsync(counts, 0, (3 + kNumBigClasses) * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, (4 + kNumBigClasses) * sizeof(uint32_t), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
-                              nullptr, nullptr);
-    uint32_t hc[3 + kNumBigClasses];
+                              nullptr, nullptr, nullptr);
+    uint32_t hc[4 + kNumBigClasses];
     SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
     // task arrays: reuse the current ones when large enough
@@ -313,11 +313,13 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
         SCAN_TRY(ensure(&d->big[c], &d->cap_big[c], d->nbig[c]));
     }
     d->nbmp = hc[1 + kNumBigClasses];
-    d->has_split = hc[2 + kNumBigClasses] > 0;
+    d->nhmid = hc[2 + kNumBigClasses];
+    d->has_split = hc[3 + kNumBigClasses] > 0;
     SCAN_TRY(ensure(&d->bmp, &d->cap_bmp, d->nbmp));
+    SCAN_TRY(ensure(&d->hmid, &d->cap_hmid, d->nhmid));
     SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
-                              d->big[1], d->big[2], d->bmp);
+                              d->big[1], d->big[2], d->bmp, d->hmid);
     SCAN_CUDA(cudaGetLastError());
     d->plan = pp;
     return SCAN_OK;
@@ -543,6 +545,7 @@ static bool g_attr_bitmap[64] = {};
 static bool g_attr_filter[64] = {};
 static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class (found once per device,
                                                 // so capturing launch_cn into a graph queries nothing)
+static int g_per_sm_hub_filter[64] = {};
 static int g_per_sm_filter[64][kNumBigClasses][2] = {};   // k_cn_filter, [class][largest class 2 at the
                                                           // default chunk, or at the autotuner's cap]
 
@@ -611,18 +614,39 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
     }
-    if (d->nbmp) {
+    // Hubs.  The mid hubs of a one-shot run go to k_cn_filter like the hash classes; the rest
+    // (and every hub when counting in full) to the hot-id bitmap kernel.
+    auto bitmap_launch = [&](const CnTask* tasks, uint32_t ntasks, uint32_t* queue) -> scan_status {
         const size_t smem = (kHotBits / 32 + kTailSlots) * sizeof(uint32_t);
         if (!g_attr_bitmap[d->device]) {
             SCAN_CUDA(cudaFuncSetAttribute(k_cn_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             g_attr_bitmap[d->device] = true;
         }
-        const uint64_t grid = std::min<uint64_t>(d->nbmp, (uint64_t)d->num_sms);
-        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(d->bmp, d->nbmp, d->task_queue + 3, d->off, d->radj,
-                                                                  d->lo_adj, d->cn,
-                                                                  d->long_words, pr, d->cn_ctr, fp);
+        const uint64_t grid = std::min<uint64_t>(ntasks, (uint64_t)d->num_sms);
+        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(tasks, ntasks, queue, d->off, d->radj, d->lo_adj,
+                                                                  d->cn, d->long_words, pr, d->cn_ctr, fp);
         ++*launches;
+        return SCAN_OK;
+    };
+    if (d->nhmid) {
+        if (filter) {
+            const int threads = 512;
+            const size_t smem = filter_smem_bytes(kHubFilterMax);
+            int& per_sm = g_per_sm_hub_filter[d->device];
+            if (per_sm == 0) {
+                SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
+                per_sm = std::max(per_sm, 1);
+            }
+            const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
+            k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->hmid, d->nhmid, kHubFilterMax, d->task_queue + 4,
+                                                              d->off, d->adj, d->lo_adj, d->cn, d->long_words, pr,
+                                                              d->cn_ctr, fp);
+            ++*launches;
+        } else {
+            SCAN_TRY(bitmap_launch(d->hmid, d->nhmid, d->task_queue + 4));
+        }
     }
+    if (d->nbmp) SCAN_TRY(bitmap_launch(d->bmp, d->nbmp, d->task_queue + 3));
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
@@ -668,7 +692,7 @@ static void cn_kernel_times(DeviceGraph* d, scan_stats* st) {
     st->ms_cn_kernel[4] = ev_ms(d->ev[11], d->ev[12]);
     st->cn_work_items[0] = d->nsmall;
     for (int c = 0; c < kNumBigClasses; ++c) st->cn_work_items[1 + c] = d->nbig[c];
-    st->cn_work_items[4] = d->nbmp;
+    st->cn_work_items[4] = d->nbmp + d->nhmid;
 }
 
 // predicate -> cores -> union-find -> attach -> classify, on cached cn.  Queued on s with
