@@ -68,11 +68,12 @@ struct DeviceGraph {
     uint32_t* hot = nullptr;       // n: hot id or kHotBits + v
     uint32_t* radj = nullptr;      // m + pad: adjacency mapped through hot[]
     uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
-    scan::CnTask* bmp = nullptr;   // hubs above kHubFilterMax
-    uint32_t nbmp = 0;
+    scan::CnTask* hubs = nullptr;  // hub tasks: hmid then bmp, one array
     scan::CnTask* hmid = nullptr;  // mid hubs (kBitmapMinDeg, kHubFilterMax]
     uint32_t nhmid = 0;
-    uint32_t cap_small = 0, cap_big[scan::kNumBigClasses] = {}, cap_bmp = 0, cap_hmid = 0;   // task array capacities
+    scan::CnTask* bmp = nullptr;   // hubs above kHubFilterMax
+    uint32_t nbmp = 0;
+    uint32_t cap_small = 0, cap_big[scan::kNumBigClasses] = {}, cap_hubs = 0;   // task array capacities
     scan::PlanParams plan{};
     uint32_t long_words = 32;      // lists of >= long_words 16-byte words get a whole warp
     uint32_t* cn = nullptr;        // E: common-neighbour counts (the serving cache)

@@ -538,12 +538,13 @@ __host__ __device__ constexpr size_t filter_smem_bytes(uint32_t entries) {
     return (size_t(1) << filter_log2bits(entries)) / 8 + size_t(entries) * 4;
 }
 
-__global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t max_entries, uint32_t* queue,
-                            const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                            const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
-                            CnPrune pr, unsigned long long* __restrict__ ctr, FusedPred fp) {
+// list_entries: capacity of the shared sorted copy (pivots hold at most that many entries).
+__global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t log2bits,
+                            uint32_t list_entries, uint32_t* queue, const uint32_t* __restrict__ off,
+                            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
+                            uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
+                            unsigned long long* __restrict__ ctr, FusedPred fp) {
     extern __shared__ __align__(16) uint32_t smem[];
-    const uint32_t log2bits = filter_log2bits(max_entries);
     const uint32_t nwords = (1u << log2bits) >> 5;
     uint32_t* bits = smem;
     uint32_t* list = smem + nwords;
@@ -553,7 +554,7 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
-        const uint32_t vb = off[tk.v], ve = off[tk.v + 1], dv = ve - vb;   // dv <= max_entries (no split)
+        const uint32_t vb = off[tk.v], ve = off[tk.v + 1], dv = ve - vb;   // dv <= list_entries (no split)
         for (uint32_t i = threadIdx.x; i < nwords / 4; i += blockDim.x)
             reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
         if (threadIdx.x == 0) next_batch = 0;

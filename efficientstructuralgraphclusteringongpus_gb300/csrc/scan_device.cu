@@ -315,8 +315,9 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
     d->nbmp = hc[1 + kNumBigClasses];
     d->nhmid = hc[2 + kNumBigClasses];
     d->has_split = hc[3 + kNumBigClasses] > 0;
-    SCAN_TRY(ensure(&d->bmp, &d->cap_bmp, d->nbmp));
-    SCAN_TRY(ensure(&d->hmid, &d->cap_hmid, d->nhmid));
+    SCAN_TRY(ensure(&d->hubs, &d->cap_hubs, d->nhmid + d->nbmp));   // mid hubs, then the larger hubs
+    d->hmid = d->hubs;
+    d->bmp = d->hubs + d->nhmid;
     SCAN_CUDA(cudaMemsetAsync(counts, 0, sizeof(hc), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, d->small_piv, d->big[0],
                               d->big[1], d->big[2], d->bmp, d->hmid);
@@ -545,7 +546,7 @@ static bool g_attr_bitmap[64] = {};
 static bool g_attr_filter[64] = {};
 static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class (found once per device,
                                                 // so capturing launch_cn into a graph queries nothing)
-static int g_per_sm_hub_filter[64] = {};
+static int g_per_sm_hub_filter[64] = {};      // k_cn_filter on the mid hubs
 static int g_per_sm_filter[64][kNumBigClasses][2] = {};   // k_cn_filter, [class][largest class 2 at the
                                                           // default chunk, or at the autotuner's cap]
 
@@ -594,9 +595,9 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
                     per_sm = std::max(per_sm, 1);
                 }
                 const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-                k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], entries, d->task_queue + c,
-                                                                  d->off, d->adj, d->lo_adj, d->cn, d->long_words,
-                                                                  pr, d->cn_ctr, fp);
+                k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], filter_log2bits(entries),
+                                                                  entries, d->task_queue + c, d->off, d->adj, d->lo_adj,
+                                                                  d->cn, d->long_words, pr, d->cn_ctr, fp);
             } else {
                 const size_t smem = big_class_slots(c) * sizeof(uint32_t);
                 int& per_sm = g_per_sm[d->device][c];
@@ -614,39 +615,43 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
         }
         SCAN_CUDA(cudaEventRecord(d->ev[9 + c], s));
     }
-    // Hubs.  The mid hubs of a one-shot run go to k_cn_filter like the hash classes; the rest
-    // (and every hub when counting in full) to the hot-id bitmap kernel.
-    auto bitmap_launch = [&](const CnTask* tasks, uint32_t ntasks, uint32_t* queue) -> scan_status {
+    // Hubs.  The mid hubs of a one-shot run go to k_cn_filter like the hash classes; the
+    // larger hubs, and every hub when counting in full, to the hot-id bitmap kernel (full
+    // counts: one launch over both task lists, d->hmid being followed by d->bmp in one array).
+    // Hubs above kHubFilterMax stay off k_cn_filter: edges between two hubs of degree above
+    // 46,339 have no early-stop threshold (the reference's int square may wrap), so the
+    // filter would end in an exact recount by binary search over the whole list.
+    uint32_t nbitmap = d->nbmp;
+    const CnTask* bitmap_tasks = d->bmp;
+    if (filter && d->nhmid) {
+        const int threads = 512;
+        const size_t smem = filter_smem_bytes(kHubFilterMax);
+        int& per_sm = g_per_sm_hub_filter[d->device];
+        if (per_sm == 0) {
+            SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
+            per_sm = std::max(per_sm, 1);
+        }
+        const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
+        k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->hmid, d->nhmid, filter_log2bits(kHubFilterMax),
+                                                          kHubFilterMax, d->task_queue + 4, d->off, d->adj,
+                                                          d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+        ++*launches;
+    } else {
+        nbitmap += d->nhmid;
+        bitmap_tasks = d->hmid;
+    }
+    if (nbitmap) {
         const size_t smem = (kHotBits / 32 + kTailSlots) * sizeof(uint32_t);
         if (!g_attr_bitmap[d->device]) {
             SCAN_CUDA(cudaFuncSetAttribute(k_cn_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             g_attr_bitmap[d->device] = true;
         }
-        const uint64_t grid = std::min<uint64_t>(ntasks, (uint64_t)d->num_sms);
-        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(tasks, ntasks, queue, d->off, d->radj, d->lo_adj,
-                                                                  d->cn, d->long_words, pr, d->cn_ctr, fp);
+        const uint64_t grid = std::min<uint64_t>(nbitmap, (uint64_t)d->num_sms);
+        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(bitmap_tasks, nbitmap, d->task_queue + 3, d->off,
+                                                                  d->radj, d->lo_adj, d->cn, d->long_words, pr,
+                                                                  d->cn_ctr, fp);
         ++*launches;
-        return SCAN_OK;
-    };
-    if (d->nhmid) {
-        if (filter) {
-            const int threads = 512;
-            const size_t smem = filter_smem_bytes(kHubFilterMax);
-            int& per_sm = g_per_sm_hub_filter[d->device];
-            if (per_sm == 0) {
-                SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
-                per_sm = std::max(per_sm, 1);
-            }
-            const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
-            k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->hmid, d->nhmid, kHubFilterMax, d->task_queue + 4,
-                                                              d->off, d->adj, d->lo_adj, d->cn, d->long_words, pr,
-                                                              d->cn_ctr, fp);
-            ++*launches;
-        } else {
-            SCAN_TRY(bitmap_launch(d->hmid, d->nhmid, d->task_queue + 4));
-        }
     }
-    if (d->nbmp) SCAN_TRY(bitmap_launch(d->bmp, d->nbmp, d->task_queue + 3));
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
     SCAN_CUDA(cudaGetLastError());
     return SCAN_OK;
