@@ -74,7 +74,8 @@ class BatchStats(C.Structure):
     _fields_ = [("ms_device", C.c_double), ("ms_total", C.c_double)] + [
         (name, C.c_uint64) for name in ("num_graphs", "num_vertices", "num_edges", "num_cores", "num_clusters")] + [
         ("graph_kernels", C.c_uint32), ("long_words", C.c_uint32), ("target_probes", C.c_uint64),
-        ("tuned_similarity_ms", C.c_double)]
+        ("tuned_similarity_ms", C.c_double), ("small_deg", C.c_uint32), ("small_batched", C.c_uint32),
+        ("hub_min_deg", C.c_uint32), ("chunk_max", C.c_uint32)]
 
 
 class ServerCounters(C.Structure):
@@ -126,6 +127,8 @@ _SIGS = {
     "scan_convert_edge_list": (C.c_int, [C.c_char_p, C.c_char_p, _u64p, _u64p]),
     "scan_eps_to_decimal": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
     "scan_graph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint32), _u64p]),
+    "scan_graph_plan": (C.c_int, [_vp, _u32p, _u32p, _u32p, _u32p]),
+    "scan_graph_set_plan": (C.c_int, [_vp, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
     "scan_cores_noalloc": (C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, C.c_uint64, C.c_char_p, C.c_int, C.c_int, _vp,
                                      _vp]),
     "scan_batch_create": (C.c_int, [C.POINTER(_vp), C.c_uint32, C.c_int, C.c_int, C.POINTER(_vp)]),
@@ -354,10 +357,22 @@ class Graph:
         return ScanResult(label, role, st.as_dict())
 
     def autotune(self, device: int = 0) -> dict:
-        """Tune the similarity stage (task size x long-list threshold) for later runs."""
+        """Tune the similarity stage's plan for later runs; returns the chosen plan."""
         ms, lw, tp = C.c_double(0), C.c_uint32(0), C.c_uint64(0)
         _check(load_library().scan_graph_autotune(self._h, device, C.byref(ms), C.byref(lw), C.byref(tp)))
-        return {"similarity_ms": ms.value, "long_words": lw.value, "target_probes": tp.value}
+        return dict(self.plan(), similarity_ms=ms.value, long_words=lw.value, target_probes=tp.value)
+
+    def set_plan(self, small_deg: int = 128, small_batched: bool = False, hub_min_deg: int = 6144,
+                 chunk_max: int = 6144, device: int = 0) -> None:
+        """Pin the similarity plan (uploads the graph first); every plan gives the same results."""
+        _check(load_library().scan_graph_set_plan(self._h, device, small_deg, int(small_batched), hub_min_deg,
+                                                  chunk_max))
+
+    def plan(self) -> dict:
+        """The resident copy's similarity plan (small-pivot cut and strategy, hub threshold, chunk)."""
+        v = [C.c_uint32(0) for _ in range(4)]
+        _check(load_library().scan_graph_plan(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("small_deg", "small_batched", "hub_min_deg", "chunk_max"), (x.value for x in v)))
 
     def common_neighbors(self, device: int = 0):
         """cn[E] in the reference edge order, plus stats."""

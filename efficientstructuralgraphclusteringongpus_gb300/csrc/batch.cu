@@ -41,6 +41,7 @@ struct scan_batch {
     cudaGraphExec_t exec = nullptr;
     uint32_t graph_launches = 0;         // kernels inside the captured graph
     float tuned_ms = 0.f;
+    bool tune_pending = false;           // autotune at the first run, with its parameters
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -123,10 +124,7 @@ scan_status scan_batch_create(const scan_graph* const* graphs, uint32_t count, i
     B_CUDA(cudaHostAlloc(&b->h_flag, sizeof(uint32_t), cudaHostAllocDefault));
     B_CUDA(cudaEventCreate(&b->ev0));
     B_CUDA(cudaEventCreate(&b->ev1));
-    if (autotune) {
-        st = autotune_similarity(b->d, &b->tuned_ms);
-        if (st != SCAN_OK) return st;
-    }
+    b->tune_pending = autotune != 0;
     *out = b.release();
     return SCAN_OK;
 }
@@ -155,19 +153,38 @@ scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const 
     B_CUDA(cudaMemcpyAsync(b->gmu, b->h_gmu, b->count * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     BatchParams bp{b->vgid, b->gpp, b->gmu};
     PredParams unused{};
+    // The pass: with no split pivot, the one-shot path of a single run (degree prune, early
+    // stop, the filter kernels, predicate fused into the counting), each pivot taking eps and
+    // the predicate from its own graph; otherwise full counts, then the predicate per graph.
+    auto similarity = [&](uint32_t* launches) -> scan_status {
+        if (d->has_split) return launch_cn(d, launches);
+        PredParams on{};   // "prune on"; every other parameter comes from the pivot's graph
+        B_CUDA(cudaMemsetAsync(d->rs.sim, 0, d->E, s));
+        B_CUDA(cudaMemsetAsync(d->rs.sd, 0, d->n * sizeof(int32_t), s));
+        B_CUDA(cudaMemsetAsync(d->rs.ctr, 0, sizeof(RunCounters), s));
+        return launch_cn(d, launches, &on, &d->rs, &bp);
+    };
+    auto queue = [&](uint32_t* launches) -> scan_status {
+        scan_status st = similarity(launches);
+        return st == SCAN_OK ? launch_cluster(d, d->rs, s, unused, 1, launches, &bp, !d->has_split) : st;
+    };
+    if (b->tune_pending) {
+        // The plan is chosen on this run's parameters; the capture below then records it.
+        scan_status st = autotune_similarity(d, &b->tuned_ms, similarity);
+        if (st != SCAN_OK) return st;
+        b->tune_pending = false;
+    }
     if (!b->exec) {
         // First run: queue once directly (sets kernel attributes), then capture the same
         // sequence into a CUDA graph for every later run.
         uint32_t launches = 0;
-        scan_status st = launch_cn(d, &launches);
-        if (st == SCAN_OK) st = launch_cluster(d, d->rs, s, unused, 1, &launches, &bp);
+        scan_status st = queue(&launches);
         if (st != SCAN_OK) return st;
         B_CUDA(cudaStreamSynchronize(s));
         cudaGraph_t graph = nullptr;
         B_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         launches = 0;
-        st = launch_cn(d, &launches);
-        if (st == SCAN_OK) st = launch_cluster(d, d->rs, s, unused, 1, &launches, &bp);
+        st = queue(&launches);
         cudaError_t ce = cudaStreamEndCapture(s, &graph);
         if (st != SCAN_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -214,6 +231,10 @@ scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const 
         stats->tuned_similarity_ms = b->tuned_ms;
         stats->long_words = d->long_words;
         stats->target_probes = d->plan.target_probes;
+        stats->small_deg = d->plan.small_deg;
+        stats->small_batched = d->plan.small_batched;
+        stats->hub_min_deg = d->plan.bitmap_min_deg;
+        stats->chunk_max = d->plan.chunk_max;
     }
     return SCAN_OK;
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -21,6 +22,9 @@ struct PlanParams {
     unsigned long long target_probes_bitmap;   // probe work per bitmap task
     uint32_t min_slice_edges;
     uint32_t chunk_max;                        // pivot entries per largest-class table (<= kChunkMaxCap)
+    uint32_t small_deg;                        // pivots up to this degree: k_cn_small (<= kSmallDeg)
+    uint32_t small_batched;                    // k_cn_small counts a batch's lists together (1) or serially
+    uint32_t bitmap_min_deg;                   // hubs: pivots above this degree (<= chunk_max)
 };
 }
 
@@ -69,7 +73,7 @@ struct DeviceGraph {
     uint32_t* radj = nullptr;      // m + pad: adjacency mapped through hot[]
     uint32_t* tailc = nullptr;     // n: non-hot neighbours per vertex
     scan::CnTask* hubs = nullptr;  // hub tasks: hmid then bmp, one array
-    scan::CnTask* hmid = nullptr;  // mid hubs (kBitmapMinDeg, kHubFilterMax]
+    scan::CnTask* hmid = nullptr;  // mid hubs (plan.bitmap_min_deg, kHubFilterMax]
     uint32_t nhmid = 0;
     scan::CnTask* bmp = nullptr;   // hubs above kHubFilterMax
     uint32_t nbmp = 0;
@@ -108,13 +112,18 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 // With `fused` (a one-shot run whose plan splits no pivot), the kernels also run the
 // predicate: sim, sd and the run counters must be zeroed before, and launch_cluster is
 // then told so (predicate_done).
+struct BatchParams;
+// bp (batched runs, with prune and fused): each pivot takes eps and the predicate from its
+// graph's entry of bp->gpp (prune then only supplies "on"); the one-shot fused path only.
 scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune = nullptr,
-                      const RunScratch* fused = nullptr);
+                      const RunScratch* fused = nullptr, const BatchParams* bp = nullptr);
 // Rebuild the similarity tasks for plan parameters pp.
 scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp);
-// Time launch_cn under a few (task size, long-list threshold) settings and keep the fastest;
-// returns the chosen setting's time in *best_ms.
-scan_status autotune_similarity(DeviceGraph* d, float* best_ms);
+// Time the similarity stage under plan settings (small-pivot strategy and degree cut, task
+// size, chunk, long-list threshold, hub threshold; a coordinate search) and keep the
+// fastest; returns its time in *best_ms.  stage (may be empty) queues the stage as the caller
+// runs it (launch_cn with full counts when empty).
+scan_status autotune_similarity(DeviceGraph* d, float* best_ms, const std::function<scan_status(uint32_t*)>& stage);
 // Per-graph parameters of a batched run (many graphs as one disjoint union): the graph of
 // each vertex and each graph's predicate parameters and mu (all device pointers).
 struct BatchParams {

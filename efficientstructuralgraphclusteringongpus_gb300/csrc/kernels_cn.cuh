@@ -24,7 +24,8 @@
 
 namespace scan {
 
-constexpr uint32_t kSmallDeg = 128;        // pivot degree handled by a single warp
+constexpr uint32_t kSmallDeg = 128;        // largest pivot degree handled by a single warp (the
+                                           // plan's small_deg may be lower)
 constexpr uint32_t kSmallSlots = 256;      // per-warp table slots (load <= 1/2)
 constexpr uint32_t kChunkMax = 6144;       // default max pivot entries staged by one CTA (load 1/4)
 constexpr uint32_t kChunkMaxCap = 12288;   // largest allowed (load 1/2 in the same table)
@@ -34,8 +35,8 @@ constexpr uint32_t kChunkMaxCap = 12288;   // largest allowed (load 1/2 in the s
 constexpr uint32_t kHotBits = 1u << 20;
 constexpr uint32_t kTailSlots = 24576;     // 96 KB; tails up to kTailMax entries (load <= 1/2)
 constexpr uint32_t kTailMax = kTailSlots / 2;
-// Pivots above kBitmapMinDeg use the bitmap path (when it is on): those the largest hash
-// table would split.  Smaller pivots stay on the hash classes, which run several CTAs per
+// Pivots above kBitmapMinDeg (the default of the plan's bitmap_min_deg) use the bitmap path
+// (when it is on): those the largest hash table would split.  Smaller pivots stay on the hash classes, which run several CTAs per
 // SM: a bitmap task of a mid-size pivot leaves most of its 32 warps waiting at the task
 // barrier (R-MAT s22, eps 0.5: 33.0 ms against 38.3 ms with the threshold at 1024).
 constexpr uint32_t kBitmapMinDeg = kChunkMax;
@@ -117,7 +118,25 @@ struct CnPrune {
     uint64_t p, q;
     uint32_t on;
     int mode;        // the run's predicate (PredParams::mode), for the fused predicate
+    // batched runs: each graph's parameters and the graph of each vertex (device memory);
+    // null for a single graph
+    const PredParams* gpp;
+    const uint32_t* vgid;
 };
+
+// The parameters for pivot v in a batched run: eps and the predicate of v's graph (the
+// graphs of a batch are one disjoint union, so both endpoints of an edge share it).
+// Kernels bind `const CnPrune& P = kPerGraph ? graph_copy : pr`, so single runs read
+// the kernel parameter itself.
+__device__ __forceinline__ CnPrune prune_of_graph(const CnPrune& pr, uint32_t v) {
+    const PredParams g = pr.gpp[pr.vgid[v]];
+    CnPrune r = pr;
+    r.eps = g.eps;
+    r.p = g.p;
+    r.q = g.q;
+    r.mode = g.mode;
+    return r;
+}
 
 // Predicate fused into the counting kernels of a one-shot run whose plan splits no pivot:
 // the count of edge k is final when its lane holds it, so the eps test, the
@@ -183,67 +202,6 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
         if (__ldg(adj + mid) < key) b = mid + 1; else e = mid;
     }
     return b;
-}
-
-// Small pivots: one warp per pivot, the pivot's list in a per-warp table.
-template <int kWarpsPerBlock>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
-           const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
-           const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, CnPrune pr,
-           unsigned long long* __restrict__ ctr, FusedPred fp) {
-    __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    uint32_t* tab = tabs[wib];
-    const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
-    unsigned long long nsim = 0, ndis = 0;
-    for (uint32_t t = blockIdx.x * kWarpsPerBlock + wib; t < npiv; t += nwarps) {
-        const uint32_t v = pivots[t];
-        const uint32_t b = off[v], e = off[v + 1];
-#pragma unroll
-        for (uint32_t i = lane; i < kSmallSlots; i += 32) tab[i] = kEmpty;
-        __syncwarp();
-        for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
-        __syncwarp();
-        const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
-        uint32_t words = 0, counted = 0;
-        // 32 lower edges at a time: lane i loads edge i's endpoint and list bounds (the
-        // dependent loads of 32 edges overlap), then the warp counts the lists one by one
-        // and lane i keeps edge i's count.
-        for (uint32_t kb = k0; kb < k1; kb += 32) {
-            const uint32_t kk = kb + lane;
-            const bool vk = kk < k1;
-            uint32_t mu_ = 0, mub = 0, mue = 0, mc = 0;
-            if (vk) {
-                mu_ = lo_adj[kk];
-                mub = off[mu_];
-                mue = off[mu_ + 1];
-                if (cn_pruned(mue - mub, e - b, pr)) mue = mub;   // cn stays 0
-            }
-            const uint32_t nk = min(32u, k1 - kb);
-            for (uint32_t i = 0; i < nk; ++i) {
-                const uint32_t ub = __shfl_sync(0xFFFFFFFFu, mub, i), ue = __shfl_sync(0xFFFFFFFFu, mue, i);
-                if (ue == ub) continue;
-                words += (ue - ub + 3u) >> 2;
-                ++counted;
-                uint32_t c = 0;
-                for (uint32_t j = ub + lane; j < ue; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
-                c = __reduce_add_sync(0xFFFFFFFFu, c);
-                if (lane == i) mc = c;
-            }
-            if (vk) cn[kk] = mc;
-            if (fp.sim) {
-                const uint32_t du = vk ? off[mu_ + 1] - off[mu_] : 0u;
-                fused_predicate(fp, pr, vk, kk, mu_, v, du, e - b, mc, lane, nsim, ndis);
-            }
-        }
-        if (lane == 0 && counted) {
-            atomicAdd(&ctr[0], (unsigned long long)words);
-            atomicAdd(&ctr[1], (unsigned long long)counted);
-        }
-        __syncwarp();
-    }
-    fused_totals(fp, lane, nsim, ndis);
 }
 
 // Larger pivots: one CTA per task; a bucketed table of `cap` slots (cap/4 buckets) in
@@ -409,6 +367,93 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
     return cnt;
 }
 
+// Small pivots: one warp per pivot, the pivot's list in a per-warp table.  Two ways to
+// count a batch of 32 lower edges (lane i loads edge i's endpoint and list bounds, so the
+// dependent loads of the 32 edges overlap); the planner picks one per graph (the autotuner
+// times both):
+//   * serial (kBatched false): the warp counts the lists one at a time, lanes over a list,
+//     one warp reduction per list;
+//   * batched: the 32 lists are streamed together by count_batch (one stream of 16-byte
+//     words, hits credited by ballot), with the early stop of a one-shot run.  The loads of
+//     different lists overlap: it pays where most edges are counted (dense graphs), and
+//     costs where the degree prune leaves few.
+__device__ __forceinline__ uint32_t small_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
+                                                     const uint32_t* tab) {
+    uint32_t c = 0;
+    if (p >= lb && p < le) c += table_has(tab, kSmallSlots, x.x);
+    if (p + 1 >= lb && p + 1 < le) c += table_has(tab, kSmallSlots, x.y);
+    if (p + 2 >= lb && p + 2 < le) c += table_has(tab, kSmallSlots, x.z);
+    if (p + 3 >= lb && p + 3 < le) c += table_has(tab, kSmallSlots, x.w);
+    return c;
+}
+
+template <int kWarpsPerBlock, bool kPerGraph, bool kBatched>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
+           const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
+           const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
+           unsigned long long* __restrict__ ctr, FusedPred fp) {
+    __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* tab = tabs[wib];
+    const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+    unsigned long long nsim = 0, ndis = 0;
+    for (uint32_t t = blockIdx.x * kWarpsPerBlock + wib; t < npiv; t += nwarps) {
+        const uint32_t v = pivots[t];
+        CnPrune Pg;
+        if constexpr (kPerGraph) Pg = prune_of_graph(pr, v);
+        const CnPrune& P = kPerGraph ? Pg : pr;
+        const uint32_t b = off[v], e = off[v + 1];
+#pragma unroll
+        for (uint32_t i = lane; i < kSmallSlots; i += 32) tab[i] = kEmpty;
+        __syncwarp();
+        for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
+        __syncwarp();
+        const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
+        uint32_t words = 0, counted = 0;
+        for (uint32_t kb = k0; kb < k1; kb += 32) {
+            const uint32_t kk = kb + lane;
+            const bool vk = kk < k1;
+            uint32_t u = 0, ub = 0, ue = 0, du = 0, mc = 0;
+            if (vk) {
+                u = lo_adj[kk];
+                ub = off[u];
+                ue = off[u + 1];
+                du = ue - ub;
+                if (cn_pruned(du, e - b, P)) ue = ub;   // cn stays 0
+            }
+            if constexpr (kBatched) {
+                const uint32_t tlo = (P.on && ue > ub) ? min_similar_count(du, e - b, P) : 0u;
+                mc = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
+                                                 [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
+                                                     return small_probe_word(x, p, lb, le, tab);
+                                                 });
+                counted += __popc(__ballot_sync(0xFFFFFFFFu, ue > ub));
+            } else {
+                const uint32_t nk = min(32u, k1 - kb);
+                for (uint32_t i = 0; i < nk; ++i) {
+                    const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, i), le = __shfl_sync(0xFFFFFFFFu, ue, i);
+                    if (le == lb) continue;
+                    words += (le - lb + 3u) >> 2;
+                    ++counted;
+                    uint32_t c = 0;
+                    for (uint32_t j = lb + lane; j < le; j += 32) c += table_has(tab, kSmallSlots, __ldg(adj + j));
+                    c = __reduce_add_sync(0xFFFFFFFFu, c);
+                    if (lane == i) mc = c;
+                }
+            }
+            if (vk) cn[kk] = mc;
+            if (fp.sim) fused_predicate(fp, P, vk, kk, u, v, du, e - b, mc, lane, nsim, ndis);
+        }
+        if (lane == 0 && counted) {
+            atomicAdd(&ctr[0], (unsigned long long)words);
+            atomicAdd(&ctr[1], (unsigned long long)counted);
+        }
+        __syncwarp();
+    }
+    fused_totals(fp, lane, nsim, ndis);
+}
+
 // Next task of a persistent CTA: from the launch's queue counter (dynamic: a CTA that drew
 // short tasks takes more), or blockIdx-strided when queue is null.  Every thread calls it;
 // it holds a CTA barrier.
@@ -539,6 +584,7 @@ __host__ __device__ constexpr size_t filter_smem_bytes(uint32_t entries) {
 }
 
 // list_entries: capacity of the shared sorted copy (pivots hold at most that many entries).
+template <bool kPerGraph>
 __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t log2bits,
                             uint32_t list_entries, uint32_t* queue, const uint32_t* __restrict__ off,
                             const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
@@ -554,6 +600,9 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
+        CnPrune Pg;
+        if constexpr (kPerGraph) Pg = prune_of_graph(pr, tk.v);
+        const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1], dv = ve - vb;   // dv <= list_entries (no split)
         for (uint32_t i = threadIdx.x; i < nwords / 4; i += blockDim.x)
             reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
@@ -579,8 +628,8 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, dv, pr)) ue = ub;
-                if (ue > ub) tlo = min_similar_count(du, dv, pr);
+                if (cn_pruned(du, dv, P)) ue = ub;
+                if (ue > ub) tlo = min_similar_count(du, dv, P);
             }
             // tlo = 0: any count may be similar, so the bound decides nothing; count exactly
             const bool bound_scan = ue > ub && tlo > 0;
@@ -604,7 +653,7 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
-            fused_predicate(fp, pr, valid, k, u, tk.v, du, dv, cnt, lane, nsim, ndis);
+            fused_predicate(fp, P, valid, k, u, tk.v, du, dv, cnt, lane, nsim, ndis);
         }
         __syncthreads();
     }
@@ -635,6 +684,7 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
 }
 
 // task.cb carries the pivot's tail size.
+template <bool kPerGraph>
 __global__ void __launch_bounds__(kBitmapThreads, 1)
 k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ radj, const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn,
@@ -650,6 +700,9 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
+        CnPrune Pg;
+        if constexpr (kPerGraph) Pg = prune_of_graph(pr, tk.v);
+        const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
         uint32_t ntb = 8;                                // tail buckets: >= tail size (load <= 1/4),
         while (ntb < tk.cb) ntb <<= 1;                   // capped at the table (load <= 1/2 there)
@@ -677,9 +730,9 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, ve - vb, pr)) ue = ub;
+                if (cn_pruned(du, ve - vb, P)) ue = ub;
             }
-            const uint32_t tlo = (pr.on && ue > ub) ? min_similar_count(ue - ub, ve - vb, pr) : 0u;
+            const uint32_t tlo = (P.on && ue > ub) ? min_similar_count(ue - ub, ve - vb, P) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlightBitmap>(radj, lane, ub, ue, tlo, long_words, words,
                                                                    [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
@@ -692,7 +745,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
-            if (fp.sim) fused_predicate(fp, pr, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
+            if (fp.sim) fused_predicate(fp, P, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
         }
         __syncthreads();
         for (uint32_t j = vb + threadIdx.x; j < ve; j += blockDim.x) {   // clear this pivot's bits
@@ -728,10 +781,10 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
         L = lo_off[v + 1] - lo_off[v];
         dv = off[v + 1] - off[v];
         if (L > 0) {
-            if (dv <= kSmallDeg) {
+            if (dv <= pp.small_deg) {
                 cls = 0;
                 ntask = 1;
-            } else if (tail && dv > kBitmapMinDeg && tail[v] <= kTailMax) {
+            } else if (tail && dv > pp.bitmap_min_deg && tail[v] <= kTailMax) {
                 cls = dv <= kHubFilterMax ? 2 + kNumBigClasses : 1 + kNumBigClasses;
                 nch = 1;
                 unsigned long long s = (work[v] + pp.target_probes_bitmap - 1) / pp.target_probes_bitmap;

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -518,6 +519,9 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     pp.target_probes_bitmap = 1ull << 25;   // bitmap tasks: 8x, each pays a CTA-wide barrier
     pp.min_slice_edges = 64;
     pp.chunk_max = kChunkMax;
+    pp.small_deg = kSmallDeg;
+    pp.small_batched = 0;
+    pp.bitmap_min_deg = kBitmapMinDeg;
     SCAN_TRY(plan_tasks(d.get(), pp));
 
     // Result and scratch arrays.
@@ -541,34 +545,33 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     return SCAN_OK;
 }
 
+// Kernel attributes and occupancies, found once per device (so capturing launch_cn into a
+// CUDA graph queries nothing).  [g] is 1 for the instantiations with per-graph parameters.
 static bool g_attr_set[64] = {};
-static bool g_attr_bitmap[64] = {};
-static bool g_attr_filter[64] = {};
-static int g_per_sm[64][kNumBigClasses] = {};   // occupancy of each hash class (found once per device,
-                                                // so capturing launch_cn into a graph queries nothing)
-static int g_per_sm_hub_filter[64] = {};      // k_cn_filter on the mid hubs
-static int g_per_sm_filter[64][kNumBigClasses][2] = {};   // k_cn_filter, [class][largest class 2 at the
-                                                          // default chunk, or at the autotuner's cap]
+static bool g_attr_bitmap[64][2] = {};
+static bool g_attr_filter[64][2] = {};
+static int g_per_sm[64][kNumBigClasses] = {};               // k_cn_big, each hash class
+static int g_per_sm_hub_filter[64][2] = {};                 // k_cn_filter on the mid hubs
+static int g_per_sm_filter[64][2][kNumBigClasses][2] = {};  // k_cn_filter, [g][class][largest class 2
+                                                            // at the default chunk, or at the cap]
 
-// cn for every edge (the similarity stage); events 7..11 bracket its four kernels.
-scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune, const RunScratch* fused) {
+template <bool kPerGraph>
+static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPrune& pr, const FusedPred& fp) {
     cudaStream_t s = d->stream;
-    CnPrune pr{0.0, 0, 1, 0u, 0};
-    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u, prune->mode};
-    FusedPred fp{nullptr, nullptr, nullptr};
-    if (fused && prune && !d->has_split) fp = FusedPred{fused->sim, fused->sd, fused->ctr};
-    SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
-    SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
-    SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
+    const int g = kPerGraph ? 1 : 0;
     SCAN_CUDA(cudaEventRecord(d->ev[7], s));
     if (d->nsmall) {
         constexpr int kWpb = 8;
-        k_cn_small<kWpb><<<grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16), kWpb * 32, 0, s>>>(
-            d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, pr, d->cn_ctr, fp);
+        const unsigned grid = (unsigned)grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16);
+        if (d->plan.small_batched)
+            k_cn_small<kWpb, kPerGraph, true><<<grid, kWpb * 32, 0, s>>>(
+                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+        else
+            k_cn_small<kWpb, kPerGraph, false><<<grid, kWpb * 32, 0, s>>>(
+                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
-    if (d->device < 0 || d->device >= 64) return fail(SCAN_ERR_INVALID_ARG, "device index must be < 64");
     if (!g_attr_set[d->device]) {
         SCAN_CUDA(cudaFuncSetAttribute(k_cn_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(big_class_slots(kNumBigClasses - 1) * sizeof(uint32_t))));
@@ -577,10 +580,10 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     // One-shot fused runs (every pivot unsplit) decide most edges from an upper bound on
     // their count (k_cn_filter); full counts and split plans use the bucketed table.
     const bool filter = fp.sim != nullptr;
-    if (filter && !g_attr_filter[d->device]) {
-        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (filter && !g_attr_filter[d->device][g]) {
+        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter<kPerGraph>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)filter_smem_bytes(kChunkMaxCap)));
-        g_attr_filter[d->device] = true;
+        g_attr_filter[d->device][g] = true;
     }
     for (int c = 0; c < kNumBigClasses; ++c) {
         if (d->nbig[c]) {
@@ -589,15 +592,16 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
                 // unsplit: class 2 pivots hold up to the plan's chunk size
                 const uint32_t entries = c == kNumBigClasses - 1 ? d->plan.chunk_max : big_class_entries(c);
                 const size_t smem = filter_smem_bytes(entries);
-                int& per_sm = g_per_sm_filter[d->device][c][entries > kChunkMax ? 1 : 0];
+                int& per_sm = g_per_sm_filter[d->device][g][c][entries > kChunkMax ? 1 : 0];
                 if (per_sm == 0) {
-                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
+                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter<kPerGraph>, threads,
+                                                                            smem));
                     per_sm = std::max(per_sm, 1);
                 }
                 const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-                k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], filter_log2bits(entries),
-                                                                  entries, d->task_queue + c, d->off, d->adj, d->lo_adj,
-                                                                  d->cn, d->long_words, pr, d->cn_ctr, fp);
+                k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
+                    d->big[c], d->nbig[c], filter_log2bits(entries), entries, d->task_queue + c, d->off, d->adj,
+                    d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
             } else {
                 const size_t smem = big_class_slots(c) * sizeof(uint32_t);
                 int& per_sm = g_per_sm[d->device][c];
@@ -626,15 +630,15 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     if (filter && d->nhmid) {
         const int threads = 512;
         const size_t smem = filter_smem_bytes(kHubFilterMax);
-        int& per_sm = g_per_sm_hub_filter[d->device];
+        int& per_sm = g_per_sm_hub_filter[d->device][g];
         if (per_sm == 0) {
-            SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter, threads, smem));
+            SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter<kPerGraph>, threads, smem));
             per_sm = std::max(per_sm, 1);
         }
         const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
-        k_cn_filter<<<(unsigned)grid, threads, smem, s>>>(d->hmid, d->nhmid, filter_log2bits(kHubFilterMax),
-                                                          kHubFilterMax, d->task_queue + 4, d->off, d->adj,
-                                                          d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+        k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
+            d->hmid, d->nhmid, filter_log2bits(kHubFilterMax), kHubFilterMax, d->task_queue + 4, d->off, d->adj,
+            d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
         ++*launches;
     } else {
         nbitmap += d->nhmid;
@@ -642,14 +646,15 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     }
     if (nbitmap) {
         const size_t smem = (kHotBits / 32 + kTailSlots) * sizeof(uint32_t);
-        if (!g_attr_bitmap[d->device]) {
-            SCAN_CUDA(cudaFuncSetAttribute(k_cn_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            g_attr_bitmap[d->device] = true;
+        if (!g_attr_bitmap[d->device][g]) {
+            SCAN_CUDA(cudaFuncSetAttribute(k_cn_bitmap<kPerGraph>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+            g_attr_bitmap[d->device][g] = true;
         }
         const uint64_t grid = std::min<uint64_t>(nbitmap, (uint64_t)d->num_sms);
-        k_cn_bitmap<<<(unsigned)grid, kBitmapThreads, smem, s>>>(bitmap_tasks, nbitmap, d->task_queue + 3, d->off,
-                                                                  d->radj, d->lo_adj, d->cn, d->long_words, pr,
-                                                                  d->cn_ctr, fp);
+        k_cn_bitmap<kPerGraph><<<(unsigned)grid, kBitmapThreads, smem, s>>>(
+            bitmap_tasks, nbitmap, d->task_queue + 3, d->off, d->radj, d->lo_adj, d->cn, d->long_words, pr,
+            d->cn_ctr, fp);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
@@ -657,31 +662,84 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     return SCAN_OK;
 }
 
-// Autotuner: try task sizes x long-list thresholds on this graph, keep the fastest.
-scan_status autotune_similarity(DeviceGraph* d, float* best_ms) {
-    const PlanParams base = d->plan;
-    const unsigned long long probes[] = {1ull << 20, 1ull << 22, 1ull << 24};
-    const uint32_t longs[] = {16, 32, 64};
-    const uint32_t chunks[] = {kChunkMax, kChunkMaxCap};
-    float best = 3.4e38f;
-    PlanParams best_pp = base;
-    uint32_t best_lw = d->long_words;
-    for (int trial = 0; trial < 6; ++trial) {
-        PlanParams pp = base;
-        pp.target_probes = probes[trial % 3];
-        pp.target_probes_bitmap = 8 * pp.target_probes;
-        pp.chunk_max = chunks[trial / 3];
+// cn for every edge (the similarity stage); events 7..12 bracket its kernels.
+scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune, const RunScratch* fused,
+                      const BatchParams* bp) {
+    if (d->device < 0 || d->device >= 64) return fail(SCAN_ERR_INVALID_ARG, "device index must be < 64");
+    CnPrune pr{0.0, 0, 1, 0u, 0, nullptr, nullptr};
+    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u, prune->mode, nullptr, nullptr};
+    const bool per_graph = prune && bp;
+    if (per_graph) {
+        pr.gpp = bp->gpp;
+        pr.vgid = bp->vgid;
+    }
+    FusedPred fp{nullptr, nullptr, nullptr};
+    if (fused && prune && !d->has_split) fp = FusedPred{fused->sim, fused->sd, fused->ctr};
+    if (per_graph && !fp.sim) return fail(SCAN_ERR_INVALID_ARG, "per-graph parameters need the fused one-shot path");
+    cudaStream_t s = d->stream;
+    SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
+    SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
+    return per_graph ? launch_cn_impl<true>(d, launches, pr, fp) : launch_cn_impl<false>(d, launches, pr, fp);
+}
+
+// Autotuner: a coordinate search over the plan, each setting timed on this graph with
+// `stage` (the similarity stage as the caller runs it; null: full counts).  In order:
+//   1. the small-pivot strategy (serial or batched lists) x the small-pivot degree cut;
+//   2. the task size x the largest hash class's chunk;
+//   3. the long-list threshold (lists of at least that many 16-byte words take a warp);
+//   4. with the bitmap path on, the hub threshold (4,096 or 6,144 entries).
+// Each step keeps the fastest setting found so far; the plan ends at the overall best.
+scan_status autotune_similarity(DeviceGraph* d, float* best_ms, const std::function<scan_status(uint32_t*)>& stage) {
+    auto run = [&](uint32_t* launches) -> scan_status {
+        return stage ? stage(launches) : launch_cn(d, launches);
+    };
+    auto time_plan = [&](const PlanParams& pp, uint32_t lw, float* ms) -> scan_status {
         SCAN_TRY(plan_tasks(d, pp));
-        for (uint32_t lw : longs) {
-            d->long_words = lw;
-            uint32_t launches = 0;
-            SCAN_TRY(launch_cn(d, &launches));   // warm
-            SCAN_CUDA(cudaEventRecord(d->ev[13], d->stream));
-            SCAN_TRY(launch_cn(d, &launches));
-            SCAN_CUDA(cudaEventRecord(d->ev[14], d->stream));
-            SCAN_CUDA(cudaEventSynchronize(d->ev[14]));
-            const float ms = ev_ms(d->ev[13], d->ev[14]);
-            if (ms < best) { best = ms; best_pp = pp; best_lw = lw; }
+        d->long_words = lw;
+        uint32_t launches = 0;
+        SCAN_TRY(run(&launches));   // warm
+        SCAN_CUDA(cudaEventRecord(d->ev[13], d->stream));
+        SCAN_TRY(run(&launches));
+        SCAN_CUDA(cudaEventRecord(d->ev[14], d->stream));
+        SCAN_CUDA(cudaEventSynchronize(d->ev[14]));
+        *ms = ev_ms(d->ev[13], d->ev[14]);
+        return SCAN_OK;
+    };
+    PlanParams best_pp = d->plan;
+    uint32_t best_lw = d->long_words;
+    float best = 3.4e38f;
+    auto consider = [&](const PlanParams& pp, uint32_t lw) -> scan_status {
+        float ms = 0.f;
+        SCAN_TRY(time_plan(pp, lw, &ms));
+        if (ms < best) { best = ms; best_pp = pp; best_lw = lw; }
+        return SCAN_OK;
+    };
+    for (uint32_t batched : {0u, 1u})
+        for (uint32_t sdeg : {64u, kSmallDeg}) {
+            PlanParams pp = best_pp;
+            pp.small_batched = batched;
+            pp.small_deg = sdeg;
+            SCAN_TRY(consider(pp, best_lw));
+        }
+    {
+        const PlanParams base = best_pp;
+        for (unsigned long long probes : {1ull << 20, 1ull << 22, 1ull << 24})
+            for (uint32_t chunk : {kChunkMax, kChunkMaxCap}) {
+                PlanParams pp = base;
+                pp.target_probes = probes;
+                pp.target_probes_bitmap = 8 * probes;
+                pp.chunk_max = chunk;
+                SCAN_TRY(consider(pp, best_lw));
+            }
+    }
+    for (uint32_t lw : {16u, 32u, 64u}) SCAN_TRY(consider(best_pp, lw));
+    if (d->tailc) {
+        const PlanParams base = best_pp;
+        for (uint32_t hub : {4096u, kBitmapMinDeg}) {
+            PlanParams pp = base;
+            pp.bitmap_min_deg = hub;
+            SCAN_TRY(consider(pp, best_lw));
         }
     }
     SCAN_TRY(plan_tasks(d, best_pp));
@@ -914,10 +972,44 @@ scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similari
     std::lock_guard<std::mutex> lock(d->mu);
     SCAN_CUDA(cudaSetDevice(d->device));
     float ms = 0.f;
-    SCAN_TRY(autotune_similarity(d, &ms));
+    SCAN_TRY(autotune_similarity(d, &ms, nullptr));
     if (best_similarity_ms) *best_similarity_ms = ms;
     if (long_words) *long_words = d->long_words;
     if (target_probes) *target_probes = d->plan.target_probes;
+    return SCAN_OK;
+}
+
+scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_batched, uint32_t* hub_min_deg,
+                            uint32_t* chunk_max) {
+    clear_error();
+    if (!g || !g->dev) return fail(SCAN_ERR_INVALID_ARG, "graph is null or not resident");
+    const PlanParams& pp = g->dev->plan;
+    if (small_deg) *small_deg = pp.small_deg;
+    if (small_batched) *small_batched = pp.small_batched;
+    if (hub_min_deg) *hub_min_deg = pp.bitmap_min_deg;
+    if (chunk_max) *chunk_max = pp.chunk_max;
+    return SCAN_OK;
+}
+
+scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_batched,
+                                uint32_t hub_min_deg, uint32_t chunk_max) {
+    clear_error();
+    if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
+    if (small_deg < 1 || small_deg > kSmallDeg || small_batched > 1 || hub_min_deg < small_deg ||
+        (chunk_max != kChunkMax && chunk_max != kChunkMaxCap))
+        return fail(SCAN_ERR_INVALID_ARG, "plan: small_deg in [1, 128], small_batched 0/1, hub_min_deg >= small_deg, "
+                                          "chunk_max 6144 or 12288");
+    SCAN_TRY(ensure_device(g, device, nullptr));
+    DeviceGraph* d = g->dev;
+    std::lock_guard<std::mutex> lock(d->mu);
+    SCAN_CUDA(cudaSetDevice(d->device));
+    PlanParams pp = d->plan;
+    pp.small_deg = small_deg;
+    pp.small_batched = small_batched;
+    pp.bitmap_min_deg = hub_min_deg;
+    pp.chunk_max = chunk_max;
+    SCAN_TRY(plan_tasks(d, pp));
+    d->cn_valid = false;
     return SCAN_OK;
 }
 

@@ -181,11 +181,24 @@ scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
                      scan_predicate predicate, int32_t* out_label, uint8_t* out_role,
                      scan_stats* stats);
 
-/* Autotune the similarity stage of the resident graph (uploading it first): times task sizes
- * x long-list thresholds x hub chunk sizes and keeps the fastest for later runs.  Outputs
- * may be NULL. */
+/* Autotune the similarity stage of the resident graph (uploading it first), timing full
+ * counts: a coordinate search over the small-pivot intersection strategy (lists counted one
+ * at a time by the warp, or a batch's lists streamed together) and degree cut, the task size
+ * and largest table chunk, the long-list threshold, and the degree above which pivots take
+ * the hub path.  The fastest plan is kept for later runs.  Outputs may be NULL. */
 scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similarity_ms,
                                 uint32_t* long_words, uint64_t* target_probes);
+
+/* The plan the similarity stage of a resident graph uses (after scan_graph_autotune, the
+ * tuned one): small-pivot degree cut, 1 when small pivots stream a batch's lists together,
+ * hub degree threshold, largest table chunk.  Outputs may be NULL. */
+scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_batched,
+                            uint32_t* hub_min_deg, uint32_t* chunk_max);
+/* Set that plan explicitly (uploading the graph first), e.g. to pin a plan tuned earlier:
+ * small_deg in [1, 128], small_batched 0 or 1, hub_min_deg >= small_deg, chunk_max 6144 or
+ * 12288.  Every plan gives the same results. */
+scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_batched,
+                                uint32_t hub_min_deg, uint32_t chunk_max);
 
 /* Exact common-neighbour count of every undirected edge, in the reference's edge order
  * (the eid / edge_u / edge_v order of scan_orient_reference): out_cn[E]. */
@@ -211,8 +224,11 @@ int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj,
 /* ---- batched SCAN: many graphs with their own (eps, mu) in one pass ------------------
  * No counterpart in the reference (it runs one graph per process).  The graphs become one
  * disjoint union on the device; one set of kernels covers all of them, captured once into a
- * CUDA graph and replayed per run.  With autotune != 0 the similarity stage's task size and
- * long-list threshold are chosen by timing on this batch.  Results equal scan_run per graph. */
+ * CUDA graph and replayed per run.  When no pivot is split, the pass is a single run's
+ * one-shot path (degree prune, early stop, predicate fused into the counting), each pivot
+ * taking eps and the predicate from its own graph.  With autotune != 0 the first run times
+ * the plan settings of scan_graph_autotune on this batch with its parameters and keeps the
+ * fastest before it captures the pass.  Results equal scan_run per graph. */
 typedef struct scan_batch scan_batch;
 
 typedef struct scan_batch_stats {
@@ -223,6 +239,10 @@ typedef struct scan_batch_stats {
     uint32_t long_words;        /* tuned long-list threshold (16-byte words)                  */
     uint64_t target_probes;     /* tuned probe work per task                                  */
     double tuned_similarity_ms; /* similarity time of the chosen setting (0 if not tuned)     */
+    uint32_t small_deg;         /* plan: small-pivot degree cut                                 */
+    uint32_t small_batched;     /* plan: 1 when small pivots stream a batch's lists together    */
+    uint32_t hub_min_deg;       /* plan: pivots above this degree take the hub path              */
+    uint32_t chunk_max;         /* plan: entries per table of the largest hash class             */
 } scan_batch_stats;
 
 scan_status scan_batch_create(const scan_graph* const* graphs, uint32_t count, int device,
