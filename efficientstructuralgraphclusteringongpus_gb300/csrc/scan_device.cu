@@ -600,7 +600,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
                 }
                 const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
                 k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
-                    d->big[c], d->nbig[c], filter_log2bits(entries), entries, d->task_queue + c, d->off, d->adj,
+                    d->big[c], d->nbig[c], entries, d->task_queue + c, d->off, d->adj,
                     d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
             } else {
                 const size_t smem = big_class_slots(c) * sizeof(uint32_t);
@@ -637,7 +637,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
         }
         const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
         k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
-            d->hmid, d->nhmid, filter_log2bits(kHubFilterMax), kHubFilterMax, d->task_queue + 4, d->off, d->adj,
+            d->hmid, d->nhmid, kHubFilterMax, d->task_queue + 4, d->off, d->adj,
             d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
         ++*launches;
     } else {
