@@ -601,7 +601,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
                 const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
                 k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
                     d->big[c], d->nbig[c], entries, d->task_queue + c, d->off, d->adj,
-                    d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+                    d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp, 0u);
             } else {
                 const size_t smem = big_class_slots(c) * sizeof(uint32_t);
                 int& per_sm = g_per_sm[d->device][c];
@@ -638,7 +638,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
         const uint64_t grid = std::min<uint64_t>(d->nhmid, (uint64_t)d->num_sms * per_sm);
         k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
             d->hmid, d->nhmid, kHubFilterMax, d->task_queue + 4, d->off, d->adj,
-            d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+            d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp, 1u);   // hubs: strided batches
         ++*launches;
     } else {
         nbitmap += d->nhmid;
@@ -654,7 +654,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
         const uint64_t grid = std::min<uint64_t>(nbitmap, (uint64_t)d->num_sms);
         k_cn_bitmap<kPerGraph><<<(unsigned)grid, kBitmapThreads, smem, s>>>(
             bitmap_tasks, nbitmap, d->task_queue + 3, d->off, d->radj, d->lo_adj, d->cn, d->long_words, pr,
-            d->cn_ctr, fp);
+            d->cn_ctr, fp, pr.on);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[12], s));
