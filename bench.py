@@ -81,7 +81,8 @@ def parse():
                     help="instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices, ~1B edges, "
                          "max degree 2M, eps 0.4, mu 5), resident and streamed under a 24 GB device cap")
     ap.add_argument("--cl-vertices", type=int, default=50_000_000)
-    ap.add_argument("--cl-edges", type=int, default=1_000_000_000)
+    ap.add_argument("--cl-edges", type=int, default=1_100_000_000,
+                    help="sampled pairs; about 1.0e9 undirected edges remain after deduplication")
     ap.add_argument("--cl-cap", type=int, default=2_000_000)
     ap.add_argument("--cl-budget-gb", type=float, default=24.0)
     return ap.parse_args()
@@ -200,6 +201,23 @@ def bench_config(args, n: int, E: int, max_degree: int, world: int) -> dict:
     return {"workload": WORKLOAD, "n": n, "undirected_edges": E, "max_degree": max_degree, "eps": args.eps,
             "mu": args.mu, "predicate": args.predicate, "parallelism": f"replicas{world}",
             "l2": "inputs larger than L2 (adjacency 4*m bytes)"}
+
+
+STAGE_PROFILE = ROOT / "profiles" / "similarity-stage_rmat-s22.md"
+
+
+def stage_traffic() -> tuple[float | None, str]:
+    """DRAM bytes of one similarity pass on this workload, from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum summed over the stage's kernels of one
+    pass); None when the summary is absent."""
+    import re
+
+    if not STAGE_PROFILE.exists():
+        return None, "no ncu summary"
+    m = re.search(r"stage_dram_bytes_per_pass\s*=\s*([0-9]+)", STAGE_PROFILE.read_text())
+    if not m:
+        return None, "no ncu summary"
+    return float(m.group(1)), f"{STAGE_PROFILE.relative_to(ROOT)} (ncu, one pass, summed over the stage's kernels)"
 
 
 def cpu_baseline(off, adj, eps: str, mu: int, mode: int) -> tuple[dict, tuple]:
@@ -568,8 +586,11 @@ def main():
 
     words = float(np.mean([s["cn_words"] for s in stats]))
     run_bytes = 16.0 * words + bm["fixed"]
+    traffic, traffic_src = stage_traffic() if (args.scale, args.edge_factor, args.seed, args.eps) == (22, 16, 1, "0.5") \
+        else (None, "no ncu summary for this configuration")
     roof = {"bound": "hbm", "achieved": run_bytes / sim_s / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": run_bytes / sim_s / 1e9 / peak, "traffic": None, "peak_source": peak_src,
+            "frac": run_bytes / sim_s / 1e9 / peak, "traffic": traffic, "traffic_source": traffic_src,
+            "peak_source": peak_src,
             "bytes": run_bytes, "list_words_read": words, "counted_edges": int(last["cn_edges_counted"]),
             "bytes_model": "16*(list words read, reported by the kernels) + 4*sum_v d_v + 20E",
             "prune_model": dict(gbs(bm["prune"]), counted_edges=bm["counted_edges"],

@@ -604,8 +604,12 @@ __host__ __device__ constexpr size_t filter_smem_bytes(uint32_t entries) {
 // expensive lower lists (those of high-degree neighbours, the ones the degree prune leaves)
 // have low ids in R-MAT-like graphs: contiguous batches would hand them to a few warps while
 // the rest finish the cheap batches and wait at the task barrier.
+// Two entry points share the body: k_cn_filter_classes (hash classes) is launch-bounded to
+// three 512-thread CTAs per SM, which holds it to 40 registers (R-MAT s22: the 4,096-entry
+// class 4.67 -> 4.25 ms); k_cn_filter (mid hubs, held to two CTAs per SM by their 112 KB of
+// shared memory) is left unbounded (48 registers; the bound measured slower there).
 template <bool kPerGraph>
-__global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t list_entries,
+__device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t list_entries,
                             uint32_t* queue, const uint32_t* __restrict__ off,
                             const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
                             uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
@@ -682,6 +686,27 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
     fused_totals(fp, lane, nsim, ndis);
 }
 
+
+template <bool kPerGraph>
+__global__ void __launch_bounds__(512, 3) k_cn_filter_classes(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t list_entries,
+                            uint32_t* queue, const uint32_t* __restrict__ off,
+                            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
+                            uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
+                            unsigned long long* __restrict__ ctr, FusedPred fp, uint32_t strided) {
+    cn_filter_body<kPerGraph>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
+                              strided);
+}
+
+template <bool kPerGraph>
+__global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t list_entries,
+                            uint32_t* queue, const uint32_t* __restrict__ off,
+                            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
+                            uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
+                            unsigned long long* __restrict__ ctr, FusedPred fp, uint32_t strided) {
+    cn_filter_body<kPerGraph>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
+                              strided);
+}
+
 // Bitmap path: one CTA of kBitmapThreads per task (pivot, edge slice), one CTA per SM.
 // Shared memory: the hot bitmap (zeroed once; each task sets its pivot's bits and clears
 // them again) and the tail table.  Probing an entry is one 4-byte shared load for hot ids.
@@ -689,14 +714,6 @@ __device__ __forceinline__ uint32_t bitmap_probe_word(const uint4 x, uint32_t p,
                                                       const uint32_t* bits, const uint32_t* tail, uint32_t ntb) {
     const uint32_t w[4] = {x.x, x.y, x.z, x.w};
     uint32_t c = 0, tails = 0;
-    if (p >= lb && p + 4u <= le && (x.x | x.y | x.z | x.w) < kHotBits) {   // inside the list, all hot
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const uint32_t word = bits[w[i] >> 5];
-            c += __funnelshift_r(word, word, w[i]) & 1u;
-        }
-        return c;
-    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const uint32_t pos = p + i;

@@ -549,7 +549,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
 // CUDA graph queries nothing).  [g] is 1 for the instantiations with per-graph parameters.
 static bool g_attr_set[64] = {};
 static bool g_attr_bitmap[64][2] = {};
-static bool g_attr_filter[64][2] = {};
+static bool g_attr_filter[64][2][2] = {};   // [g][mid hubs]
 static int g_per_sm[64][kNumBigClasses] = {};               // k_cn_big, each hash class
 static int g_per_sm_hub_filter[64][2] = {};                 // k_cn_filter on the mid hubs
 static int g_per_sm_filter[64][2][kNumBigClasses][2] = {};  // k_cn_filter, [g][class][largest class 2
@@ -580,10 +580,12 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
     // One-shot fused runs (every pivot unsplit) decide most edges from an upper bound on
     // their count (k_cn_filter); full counts and split plans use the bucketed table.
     const bool filter = fp.sim != nullptr;
-    if (filter && !g_attr_filter[d->device][g]) {
-        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter<kPerGraph>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (filter && !g_attr_filter[d->device][g][0]) {
+        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter_classes<kPerGraph>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)filter_smem_bytes(kChunkMaxCap)));
-        g_attr_filter[d->device][g] = true;
+        SCAN_CUDA(cudaFuncSetAttribute(k_cn_filter<kPerGraph>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)filter_smem_bytes(kHubFilterMax)));
+        g_attr_filter[d->device][g][0] = true;
     }
     for (int c = 0; c < kNumBigClasses; ++c) {
         if (d->nbig[c]) {
@@ -594,12 +596,12 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
                 const size_t smem = filter_smem_bytes(entries);
                 int& per_sm = g_per_sm_filter[d->device][g][c][entries > kChunkMax ? 1 : 0];
                 if (per_sm == 0) {
-                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter<kPerGraph>, threads,
-                                                                            smem));
+                    SCAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cn_filter_classes<kPerGraph>,
+                                                                            threads, smem));
                     per_sm = std::max(per_sm, 1);
                 }
                 const uint64_t grid = std::min<uint64_t>(d->nbig[c], (uint64_t)d->num_sms * per_sm);
-                k_cn_filter<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
+                k_cn_filter_classes<kPerGraph><<<(unsigned)grid, threads, smem, s>>>(
                     d->big[c], d->nbig[c], entries, d->task_queue + c, d->off, d->adj,
                     d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp, 0u);
             } else {
