@@ -377,6 +377,8 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
 //     words, hits credited by ballot), with the early stop of a one-shot run.  The loads of
 //     different lists overlap: it pays where most edges are counted (dense graphs), and
 //     costs where the degree prune leaves few.
+// Warps draw pivots from a queue counter (`queue`, zeroed before the launch): pivots differ
+// widely in cost, and a fixed stride left a tail (R-MAT s22: 1.40 -> 0.99 ms).
 __device__ __forceinline__ uint32_t small_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
                                                      const uint32_t* tab) {
     uint32_t c = 0;
@@ -392,13 +394,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
            const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
-           unsigned long long* __restrict__ ctr, FusedPred fp) {
+           unsigned long long* __restrict__ ctr, FusedPred fp, uint32_t* queue) {
     __shared__ uint32_t tabs[kWarpsPerBlock][kSmallSlots];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* tab = tabs[wib];
-    const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
     unsigned long long nsim = 0, ndis = 0;
-    for (uint32_t t = blockIdx.x * kWarpsPerBlock + wib; t < npiv; t += nwarps) {
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(queue, 1u);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        if (t >= npiv) break;
         const uint32_t v = pivots[t];
         CnPrune Pg;
         if constexpr (kPerGraph) Pg = prune_of_graph(pr, v);

@@ -565,10 +565,12 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
         const unsigned grid = (unsigned)grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16);
         if (d->plan.small_batched)
             k_cn_small<kWpb, kPerGraph, true><<<grid, kWpb * 32, 0, s>>>(
-                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp,
+                d->task_queue + 5);
         else
             k_cn_small<kWpb, kPerGraph, false><<<grid, kWpb * 32, 0, s>>>(
-                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp);
+                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp,
+                d->task_queue + 5);
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
