@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--eps", default="0.5")
     ap.add_argument("--mu", type=int, default=5)
     ap.add_argument("--predicate", default="ref-f64", choices=["ref-f64", "exact"])
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the oracle pass (and the parity check)")
     ap.add_argument("--no-reference-kernels", action="store_true",
                     help="with --impl reference: skip the reference's GPU kernels context field")
