@@ -17,9 +17,11 @@ cores, union-find, attach, hub/outlier) over the graph.
   sweep     eps in {0.2, 0.4, 0.6, 0.8} x mu in {2, 5, 10} on the same resident graph
   serving / batch   the serving loop and the batched small graphs (their own configs)
 
-  --chung-lu  instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices,
-              ~1B undirected edges, max degree 2M, eps 0.4, mu 5), resident and streamed
-              under a 24 GB device cap (several minutes; not part of the default run)
+  chung_lu  the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices, ~1.0B
+            undirected edges, max degree cap 2M, eps 0.4, mu 5): resident, then streamed
+            under a 24 GB device cap, labels compared (--chung-lu-runs resident runs, one
+            streamed; --no-chung-lu skips it)
+  --chung-lu  only that block, with --steps runs each
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has
@@ -77,6 +79,8 @@ def parse():
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--batch-max-n", type=int, default=100000)
     ap.add_argument("--no-sweep", action="store_true", help="skip the eps x mu sweep on the bench graph")
+    ap.add_argument("--no-chung-lu", action="store_true", help="skip the skewed hub-heavy block of the default run")
+    ap.add_argument("--chung-lu-runs", type=int, default=2, help="timed runs of the Chung-Lu block in the default run")
     ap.add_argument("--chung-lu", action="store_true",
                     help="instead: the skewed hub-heavy config (Chung-Lu, exponent 2.1, 50M vertices, ~1B edges, "
                          "max degree 2M, eps 0.4, mu 5), resident and streamed under a 24 GB device cap")
@@ -451,7 +455,7 @@ def sweep_bench(g, args, mode, device: int) -> list:
     return out
 
 
-def chung_lu_bench(args, device: int) -> dict:
+def chung_lu_bench(args, device: int, runs_resident: int, runs_streamed: int) -> dict:
     """Skewed hub-heavy config: the graph resident in HBM, then streamed (adjacency in pinned
     host memory read over the host link, the rest under a device cap); labels must agree."""
     import efficientstructuralgraphclusteringongpus_gb300 as sg
@@ -465,9 +469,9 @@ def chung_lu_bench(args, device: int) -> dict:
            "undirected_edges": g.num_edges, "max_degree": g.max_degree, "eps": eps, "mu": mu,
            "predicate": args.predicate, "generate_s": gen_s}
 
-    def timed(tag):
+    def timed(tag, k):
         g.run(eps, mu, mode, device=device)
-        runs = [g.run(eps, mu, mode, device=device) for _ in range(max(args.steps, 1))]
+        runs = [g.run(eps, mu, mode, device=device) for _ in range(max(k, 1))]
         ms = [r.stats["ms_similarity"] + r.stats["ms_cluster"] for r in runs]
         st = runs[-1].stats
         out[tag] = {"ms_per_step": float(np.mean(ms)), "edges_per_s": g.num_edges / (float(np.mean(ms)) / 1e3),
@@ -478,12 +482,12 @@ def chung_lu_bench(args, device: int) -> dict:
     t = time.perf_counter()
     g.upload(device)
     out["upload_s"] = time.perf_counter() - t
-    lab = timed("resident")
+    lab = timed("resident", runs_resident)
     g.release_device()
     t = time.perf_counter()
     used = g.upload_streamed(device, int(args.cl_budget_gb * (1 << 30)))
     out["streamed_upload_s"] = time.perf_counter() - t
-    lab2 = timed("streamed")
+    lab2 = timed("streamed", runs_streamed)
     out["streamed"]["budget_bytes"] = int(args.cl_budget_gb * (1 << 30))
     out["streamed"]["device_bytes_used"] = used
     out["streamed_labels_equal_resident"] = bool(np.array_equal(lab, lab2))
@@ -507,7 +511,7 @@ def main():
     mode = sg.PRED_REF_F64 if args.predicate == "ref-f64" else sg.PRED_EXACT
     if args.chung_lu:
         if rank == 0:
-            print(json.dumps({"chung_lu": chung_lu_bench(args, local)}))
+            print(json.dumps({"chung_lu": chung_lu_bench(args, local, args.steps, args.steps)}))
         dist.close()
         return
     if args.serving_only or args.batch_only:
@@ -620,6 +624,7 @@ def main():
         sweep = None if args.no_sweep else sweep_bench(g, args, mode, local)
         serving = None if args.no_serving else serving_bench(args, local)
         batch = None if args.no_batch else batch_bench(args, local)
+        chung = None if args.no_chung_lu else chung_lu_bench(args, local, args.chung_lu_runs, 1)
         result = {
             "metric": "similarity edges/s", "value": value, "unit": "similarity edges/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -640,6 +645,7 @@ def main():
             "sweep": sweep,
             "serving": serving,
             "batch": batch,
+            "chung_lu": chung,
             "stages_ms": {"similarity": float(np.mean(sim_ms)),
                           "cluster": float(np.mean([s["ms_cluster"] for s in stats])),
                           "d2h": float(np.mean([s["ms_d2h"] for s in stats])),
