@@ -4,19 +4,22 @@
 // in the longer one (GPUSCAN++/GPUScan.cu:174-222), once per edge and again lazily in
 // the link and attach phases (:579-584, :701-706).  Here every edge is counted exactly
 // once, grouped by its higher endpoint v (the pivot):
-//   1. the pivot's list N(v) (or one id-range chunk of it) is inserted into an
-//      open-addressing hash table in shared memory (load factor <= 1/4; the CTA-wide
-//      kernel uses 4-slot buckets read with one 16-byte load);
+//   1. the pivot's list N(v) (or one id-range chunk of it) is staged in shared memory: a
+//      per-warp hash table for small pivots, and per CTA task a hashed bitmap plus a sorted
+//      copy (one-shot runs, k_cn_filter), a bucketed hash table (full counts, k_cn_big) or
+//      a bitmap of hot ids (hubs, k_cn_bitmap);
 //   2. warps stream the lower endpoints' lists N(u) with 16-byte loads and probe each
-//      element against the table; a warp reduction gives the count.
+//      element against it; ballots and warp reductions give the counts.
 // Per edge this reads deg(u) <= deg(v) entries, the shorter list, once; the longer
 // list is read once per task, not once per edge.
 //
-// Work is cut into tasks (pivot, chunk of N(v), slice of the pivot's edges):
-//   * small pivots (deg <= kSmallDeg): one warp per pivot, a 256-slot table per warp;
-//   * larger pivots: one CTA per task; pivots above kChunkMax entries are split into
-//     id-range chunks, each probed by the matching sub-range of N(u) (binary search),
-//     and the partial counts are added atomically.
+// Work is cut into tasks (pivot, chunk of N(v), slice of the pivot's edges) by k_plan:
+//   * small pivots (degree <= the plan's small_deg): one warp per pivot (k_cn_small);
+//   * larger pivots: one CTA per task, by size class; hubs above the plan's hub threshold
+//     take the hub task list;
+//   * with the bitmap path off, pivots above the plan's chunk are split into id-range
+//     chunks, each probed by the matching sub-range of N(u) (binary search), and the
+//     partial counts are added atomically.
 #pragma once
 
 #include "device_common.cuh"

@@ -5,8 +5,9 @@
 // Pipeline (reference stages in GPUSCAN++/GPUScan.cu:800-1009 for comparison):
 //   upload     H2D of CSR, device-side input checks     (:836-851; checks of Graph.cpp:270-288)
 //   orient     lower-list construction                   (host getEidAndEdgeList, Graph.cpp:52-141)
-//   similarity cn for every edge (k_cn_small/k_cn_big)   (__check_core + lazy intersect, :276-367)
-//   predicate  eps test + similar-degree counts          (__prep_edge/__check_core, :133-172)
+//   similarity cn for every edge (kernels_cn.cuh)        (__check_core + lazy intersect, :276-367)
+//   predicate  eps test + similar-degree counts, fused    (__prep_edge/__check_core, :133-172)
+//              into the counting in one-shot runs
 //   cluster    cores, union-find, flatten                (__cluster_core1/2, __cluster_core, :479-652)
 //   attach     borders                                   (__cluster_noncore, :654-730)
 //   classify   hubs / outliers                           (__classify_others, :732-798)

@@ -101,8 +101,9 @@ def test_isolated_and_empty_edges():
 
 
 # ---- generated graphs -------------------------------------------------------------------
-# By default pivots above degree 1024 take the bitmap kernel; "off" forces the hash-table
-# classes and the chunked hub path on the same graphs.
+# By default pivots above degree 6,144 take the hub paths (the filter kernel up to 12,288
+# entries in one-shot runs, the hot-id bitmap kernel above it and for full counts); "off"
+# forces the hash-table classes and the chunked hub path on the same graphs.
 @pytest.fixture(params=["default", "off"])
 def bitmap(request, monkeypatch):
     if request.param == "default":
