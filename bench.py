@@ -344,7 +344,7 @@ def batch_bench(args, device: int) -> dict:
                       "ms_call": float(np.median([r["ms_total"] for r in runs])),
                       "graph_kernels": runs[-1]["graph_kernels"], "long_words": runs[-1]["long_words"],
                       "target_probes": runs[-1]["target_probes"],
-                      "tuned_plan": {k: runs[-1][k] for k in ("small_deg", "small_batched", "hub_min_deg", "chunk_max")}}
+                      "tuned_plan": {k: runs[-1][k] for k in ("small_deg", "small_strategy", "hub_min_deg", "chunk_max")}}
     # one scan_run per graph, every graph already resident
     for g in graphs:
         g.upload(device)

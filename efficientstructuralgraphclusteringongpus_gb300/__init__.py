@@ -23,11 +23,13 @@ import numpy as np
 
 __all__ = [
     "ScanError", "Graph", "ScanStats", "GPUScan", "count_clusters", "library_path", "load_library",
-    "cores_noalloc", "Server", "Batch", "convert_edge_list", "PRED_EXACT", "PRED_REF_F64", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
+    "cores_noalloc", "Server", "Batch", "convert_edge_list", "PRED_EXACT", "PRED_REF_F64", "SMALL_SERIAL", "SMALL_BATCHED", "SMALL_SEARCH", "ROLE_OUTLIER", "ROLE_HUB", "ROLE_BORDER", "ROLE_CORE", "EXPORTED_SYMBOLS",
 ]
 
 PRED_EXACT = 0
 PRED_REF_F64 = 1
+# small-pivot intersection strategies of the similarity plan
+SMALL_SERIAL, SMALL_BATCHED, SMALL_SEARCH = 0, 1, 2
 ROLE_OUTLIER, ROLE_HUB, ROLE_BORDER, ROLE_CORE = 0, 1, 2, 3
 
 _PKG = Path(__file__).resolve().parent
@@ -74,7 +76,7 @@ class BatchStats(C.Structure):
     _fields_ = [("ms_device", C.c_double), ("ms_total", C.c_double)] + [
         (name, C.c_uint64) for name in ("num_graphs", "num_vertices", "num_edges", "num_cores", "num_clusters")] + [
         ("graph_kernels", C.c_uint32), ("long_words", C.c_uint32), ("target_probes", C.c_uint64),
-        ("tuned_similarity_ms", C.c_double), ("small_deg", C.c_uint32), ("small_batched", C.c_uint32),
+        ("tuned_similarity_ms", C.c_double), ("small_deg", C.c_uint32), ("small_strategy", C.c_uint32),
         ("hub_min_deg", C.c_uint32), ("chunk_max", C.c_uint32)]
 
 
@@ -362,17 +364,18 @@ class Graph:
         _check(load_library().scan_graph_autotune(self._h, device, C.byref(ms), C.byref(lw), C.byref(tp)))
         return dict(self.plan(), similarity_ms=ms.value, long_words=lw.value, target_probes=tp.value)
 
-    def set_plan(self, small_deg: int = 128, small_batched: bool = False, hub_min_deg: int = 6144,
+    def set_plan(self, small_deg: int = 128, small_strategy: int = SMALL_SERIAL, hub_min_deg: int = 6144,
                  chunk_max: int = 6144, device: int = 0) -> None:
-        """Pin the similarity plan (uploads the graph first); every plan gives the same results."""
-        _check(load_library().scan_graph_set_plan(self._h, device, small_deg, int(small_batched), hub_min_deg,
+        """Pin the similarity plan (uploads the graph first); every plan gives the same results.
+        small_strategy: SMALL_SERIAL, SMALL_BATCHED or SMALL_SEARCH."""
+        _check(load_library().scan_graph_set_plan(self._h, device, small_deg, int(small_strategy), hub_min_deg,
                                                   chunk_max))
 
     def plan(self) -> dict:
         """The resident copy's similarity plan (small-pivot cut and strategy, hub threshold, chunk)."""
         v = [C.c_uint32(0) for _ in range(4)]
         _check(load_library().scan_graph_plan(self._h, *[C.byref(x) for x in v]))
-        return dict(zip(("small_deg", "small_batched", "hub_min_deg", "chunk_max"), (x.value for x in v)))
+        return dict(zip(("small_deg", "small_strategy", "hub_min_deg", "chunk_max"), (x.value for x in v)))
 
     def common_neighbors(self, device: int = 0):
         """cn[E] in the reference edge order, plus stats."""

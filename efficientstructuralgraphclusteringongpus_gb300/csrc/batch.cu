@@ -232,7 +232,7 @@ scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const 
         stats->long_words = d->long_words;
         stats->target_probes = d->plan.target_probes;
         stats->small_deg = d->plan.small_deg;
-        stats->small_batched = d->plan.small_batched;
+        stats->small_strategy = d->plan.small_strategy;
         stats->hub_min_deg = d->plan.bitmap_min_deg;
         stats->chunk_max = d->plan.chunk_max;
     }

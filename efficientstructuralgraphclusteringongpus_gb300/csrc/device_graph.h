@@ -23,7 +23,7 @@ struct PlanParams {
     uint32_t min_slice_edges;
     uint32_t chunk_max;                        // pivot entries per largest-class table (<= kChunkMaxCap)
     uint32_t small_deg;                        // pivots up to this degree: k_cn_small (<= kSmallDeg)
-    uint32_t small_batched;                    // k_cn_small counts a batch's lists together (1) or serially
+    uint32_t small_strategy;                   // k_cn_small: 0 serial hash, 1 batched hash, 2 batched search
     uint32_t bitmap_min_deg;                   // hubs: pivots above this degree (<= chunk_max)
 };
 }

@@ -370,18 +370,42 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
     return cnt;
 }
 
-// Small pivots: one warp per pivot, the pivot's list in a per-warp table.  Two ways to
-// count a batch of 32 lower edges (lane i loads edge i's endpoint and list bounds, so the
-// dependent loads of the 32 edges overlap); the planner picks one per graph (the autotuner
-// times both):
-//   * serial (kBatched false): the warp counts the lists one at a time, lanes over a list,
-//     one warp reduction per list;
-//   * batched: the 32 lists are streamed together by count_batch (one stream of 16-byte
-//     words, hits credited by ballot), with the early stop of a one-shot run.  The loads of
-//     different lists overlap: it pays where most edges are counted (dense graphs), and
-//     costs where the degree prune leaves few.
+// Small pivots: one warp per pivot.  Three ways to count a batch of 32 lower edges (lane i
+// loads edge i's endpoint and list bounds, so the dependent loads of the 32 edges overlap);
+// the planner picks one per graph (the autotuner times them):
+//   * kSmallSerial: the pivot's list in a per-warp hash table; the warp counts the lists one
+//     at a time, lanes over a list, one warp reduction per list;
+//   * kSmallBatched: the same table; the 32 lists are streamed together by count_batch (one
+//     stream of 16-byte words, hits credited by ballot and popc), with the early stop of a
+//     one-shot run.  The loads of different lists overlap: it pays where most edges are
+//     counted (dense graphs), and costs where the degree prune leaves few;
+//   * kSmallSearch: as kSmallBatched, but the pivot's list is kept sorted and each entry is
+//     found by binary search (a galloping intersection, the reference's own method,
+//     GPUSCAN++/GPUScan.cu:174-222, inside the warp-cooperative stream): no table to clear
+//     or fill, log2(deg) dependent probes per entry.
 // Warps draw pivots from a queue counter (`queue`, zeroed before the launch): pivots differ
 // widely in cost, and a fixed stride left a tail (R-MAT s22: 1.40 -> 0.99 ms).
+constexpr int kSmallSerial = 0, kSmallBatched = 1, kSmallSearch = 2;
+
+__device__ __forceinline__ uint32_t sorted_has(const uint32_t* list, uint32_t n, uint32_t w) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (list[mid] < w) lo = mid + 1; else hi = mid;
+    }
+    return (lo < n && list[lo] == w) ? 1u : 0u;
+}
+
+__device__ __forceinline__ uint32_t search_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
+                                                      const uint32_t* list, uint32_t n) {
+    uint32_t c = 0;
+    if (p >= lb && p < le) c += sorted_has(list, n, x.x);
+    if (p + 1 >= lb && p + 1 < le) c += sorted_has(list, n, x.y);
+    if (p + 2 >= lb && p + 2 < le) c += sorted_has(list, n, x.z);
+    if (p + 3 >= lb && p + 3 < le) c += sorted_has(list, n, x.w);
+    return c;
+}
+
 __device__ __forceinline__ uint32_t small_probe_word(const uint4 x, uint32_t p, uint32_t lb, uint32_t le,
                                                      const uint32_t* tab) {
     uint32_t c = 0;
@@ -392,7 +416,7 @@ __device__ __forceinline__ uint32_t small_probe_word(const uint4 x, uint32_t p, 
     return c;
 }
 
-template <int kWarpsPerBlock, bool kPerGraph, bool kBatched>
+template <int kWarpsPerBlock, bool kPerGraph, int kStrategy>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* __restrict__ off,
            const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_off,
@@ -412,10 +436,14 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
         if constexpr (kPerGraph) Pg = prune_of_graph(pr, v);
         const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t b = off[v], e = off[v + 1];
+        if constexpr (kStrategy == kSmallSearch) {
+            for (uint32_t j = b + lane; j < e; j += 32) tab[j - b] = adj[j];   // sorted copy (e - b <= 128)
+        } else {
 #pragma unroll
-        for (uint32_t i = lane; i < kSmallSlots; i += 32) tab[i] = kEmpty;
-        __syncwarp();
-        for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
+            for (uint32_t i = lane; i < kSmallSlots; i += 32) tab[i] = kEmpty;
+            __syncwarp();
+            for (uint32_t j = b + lane; j < e; j += 32) table_insert(tab, kSmallSlots, adj[j]);
+        }
         __syncwarp();
         const uint32_t k0 = lo_off[v], k1 = lo_off[v + 1];
         uint32_t words = 0, counted = 0;
@@ -430,11 +458,14 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
                 du = ue - ub;
                 if (cn_pruned(du, e - b, P)) ue = ub;   // cn stays 0
             }
-            if constexpr (kBatched) {
+            if constexpr (kStrategy != kSmallSerial) {
                 const uint32_t tlo = (P.on && ue > ub) ? min_similar_count(du, e - b, P) : 0u;
                 mc = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                  [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
-                                                     return small_probe_word(x, p, lb, le, tab);
+                                                     if constexpr (kStrategy == kSmallSearch)
+                                                         return search_probe_word(x, p, lb, le, tab, e - b);
+                                                     else
+                                                         return small_probe_word(x, p, lb, le, tab);
                                                  });
                 counted += __popc(__ballot_sync(0xFFFFFFFFu, ue > ub));
             } else {

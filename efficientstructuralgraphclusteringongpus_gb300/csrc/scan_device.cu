@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <type_traits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -521,7 +522,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     pp.min_slice_edges = 64;
     pp.chunk_max = kChunkMax;
     pp.small_deg = kSmallDeg;
-    pp.small_batched = 0;
+    pp.small_strategy = kSmallSerial;
     pp.bitmap_min_deg = kBitmapMinDeg;
     SCAN_TRY(plan_tasks(d.get(), pp));
 
@@ -564,14 +565,14 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
     if (d->nsmall) {
         constexpr int kWpb = 8;
         const unsigned grid = (unsigned)grid_for(d, (uint64_t)d->nsmall * 32, kWpb * 32, 16);
-        if (d->plan.small_batched)
-            k_cn_small<kWpb, kPerGraph, true><<<grid, kWpb * 32, 0, s>>>(
+        auto launch_small = [&](auto strategy) {
+            k_cn_small<kWpb, kPerGraph, decltype(strategy)::value><<<grid, kWpb * 32, 0, s>>>(
                 d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp,
                 d->task_queue + 5);
-        else
-            k_cn_small<kWpb, kPerGraph, false><<<grid, kWpb * 32, 0, s>>>(
-                d->small_piv, d->nsmall, d->off, d->adj, d->lo_off, d->lo_adj, d->cn, d->long_words, pr, d->cn_ctr, fp,
-                d->task_queue + 5);
+        };
+        if (d->plan.small_strategy == kSmallBatched) launch_small(std::integral_constant<int, kSmallBatched>());
+        else if (d->plan.small_strategy == kSmallSearch) launch_small(std::integral_constant<int, kSmallSearch>());
+        else launch_small(std::integral_constant<int, kSmallSerial>());
         ++*launches;
     }
     SCAN_CUDA(cudaEventRecord(d->ev[8], s));
@@ -720,10 +721,10 @@ scan_status autotune_similarity(DeviceGraph* d, float* best_ms, const std::funct
         if (ms < best) { best = ms; best_pp = pp; best_lw = lw; }
         return SCAN_OK;
     };
-    for (uint32_t batched : {0u, 1u})
+    for (uint32_t strategy : {(uint32_t)kSmallSerial, (uint32_t)kSmallBatched, (uint32_t)kSmallSearch})
         for (uint32_t sdeg : {64u, kSmallDeg}) {
             PlanParams pp = best_pp;
-            pp.small_batched = batched;
+            pp.small_strategy = strategy;
             pp.small_deg = sdeg;
             SCAN_TRY(consider(pp, best_lw));
         }
@@ -984,25 +985,25 @@ scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similari
     return SCAN_OK;
 }
 
-scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_batched, uint32_t* hub_min_deg,
+scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_strategy, uint32_t* hub_min_deg,
                             uint32_t* chunk_max) {
     clear_error();
     if (!g || !g->dev) return fail(SCAN_ERR_INVALID_ARG, "graph is null or not resident");
     const PlanParams& pp = g->dev->plan;
     if (small_deg) *small_deg = pp.small_deg;
-    if (small_batched) *small_batched = pp.small_batched;
+    if (small_strategy) *small_strategy = pp.small_strategy;
     if (hub_min_deg) *hub_min_deg = pp.bitmap_min_deg;
     if (chunk_max) *chunk_max = pp.chunk_max;
     return SCAN_OK;
 }
 
-scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_batched,
+scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_strategy,
                                 uint32_t hub_min_deg, uint32_t chunk_max) {
     clear_error();
     if (!g) return fail(SCAN_ERR_INVALID_ARG, "graph is null");
-    if (small_deg < 1 || small_deg > kSmallDeg || small_batched > 1 || hub_min_deg < small_deg ||
+    if (small_deg < 1 || small_deg > kSmallDeg || small_strategy > 2 || hub_min_deg < small_deg ||
         (chunk_max != kChunkMax && chunk_max != kChunkMaxCap))
-        return fail(SCAN_ERR_INVALID_ARG, "plan: small_deg in [1, 128], small_batched 0/1, hub_min_deg >= small_deg, "
+        return fail(SCAN_ERR_INVALID_ARG, "plan: small_deg in [1, 128], small_strategy 0-2, hub_min_deg >= small_deg, "
                                           "chunk_max 6144 or 12288");
     SCAN_TRY(ensure_device(g, device, nullptr));
     DeviceGraph* d = g->dev;
@@ -1010,7 +1011,7 @@ scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, u
     SCAN_CUDA(cudaSetDevice(d->device));
     PlanParams pp = d->plan;
     pp.small_deg = small_deg;
-    pp.small_batched = small_batched;
+    pp.small_strategy = small_strategy;
     pp.bitmap_min_deg = hub_min_deg;
     pp.chunk_max = chunk_max;
     SCAN_TRY(plan_tasks(d, pp));

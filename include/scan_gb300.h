@@ -184,21 +184,23 @@ scan_status scan_run(scan_graph* g, int device, const char* eps_decimal, int mu,
 
 /* Autotune the similarity stage of the resident graph (uploading it first), timing full
  * counts: a coordinate search over the small-pivot intersection strategy (lists counted one
- * at a time by the warp, or a batch's lists streamed together) and degree cut, the task size
+ * at a time through a hash table, a batch's lists streamed through it, or streamed with
+ * binary search in the sorted list) and degree cut, the task size
  * and largest table chunk, the long-list threshold, and the degree above which pivots take
  * the hub path.  The fastest plan is kept for later runs.  Outputs may be NULL. */
 scan_status scan_graph_autotune(scan_graph* g, int device, double* best_similarity_ms,
                                 uint32_t* long_words, uint64_t* target_probes);
 
 /* The plan the similarity stage of a resident graph uses (after scan_graph_autotune, the
- * tuned one): small-pivot degree cut, 1 when small pivots stream a batch's lists together,
- * hub degree threshold, largest table chunk.  Outputs may be NULL. */
-scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_batched,
+ * tuned one): small-pivot degree cut, small-pivot strategy (0 serial hash table, 1 batched
+ * hash table, 2 batched binary search), hub degree threshold, largest table chunk.  Outputs
+ * may be NULL. */
+scan_status scan_graph_plan(const scan_graph* g, uint32_t* small_deg, uint32_t* small_strategy,
                             uint32_t* hub_min_deg, uint32_t* chunk_max);
 /* Set that plan explicitly (uploading the graph first), e.g. to pin a plan tuned earlier:
- * small_deg in [1, 128], small_batched 0 or 1, hub_min_deg >= small_deg, chunk_max 6144 or
+ * small_deg in [1, 128], small_strategy 0-2, hub_min_deg >= small_deg, chunk_max 6144 or
  * 12288.  Every plan gives the same results. */
-scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_batched,
+scan_status scan_graph_set_plan(scan_graph* g, int device, uint32_t small_deg, uint32_t small_strategy,
                                 uint32_t hub_min_deg, uint32_t chunk_max);
 
 /* Exact common-neighbour count of every undirected edge, in the reference's edge order
@@ -241,7 +243,9 @@ typedef struct scan_batch_stats {
     uint64_t target_probes;     /* tuned probe work per task                                  */
     double tuned_similarity_ms; /* similarity time of the chosen setting (0 if not tuned)     */
     uint32_t small_deg;         /* plan: small-pivot degree cut                                 */
-    uint32_t small_batched;     /* plan: 1 when small pivots stream a batch's lists together    */
+    uint32_t small_strategy;    /* plan: small-pivot intersection, 0 serial hash table, 1 a
+                                   batch's lists streamed through the table, 2 streamed with
+                                   binary search in the sorted list                            */
     uint32_t hub_min_deg;       /* plan: pivots above this degree take the hub path              */
     uint32_t chunk_max;         /* plan: entries per table of the largest hash class             */
 } scan_batch_stats;
