@@ -52,6 +52,8 @@ struct DeviceGraph {
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;   // the hub kernels of the similarity stage, beside the classes
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t n = 0;
     uint64_t m = 0, E = 0;
     uint32_t* off = nullptr;
@@ -89,7 +91,7 @@ struct DeviceGraph {
     std::vector<std::pair<void*, size_t>> allocs;   // (pointer, bytes), returned to the cache on free
     uint64_t device_bytes = 0;     // device memory held by this graph
     uint32_t* adj_host = nullptr;  // streamed mode: pinned, GPU-mapped adjacency (adj points into it)
-    cudaEvent_t ev[16] = {};       // 0-2 upload, 3-6 run stages, 7-12 similarity kernels
+    cudaEvent_t ev[16] = {};       // 0-2 upload, 3-6 run stages, 7-12 and 15 similarity kernels
     std::mutex mu;                 // one run at a time per resident graph
 };
 

@@ -215,10 +215,11 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 // loads of 32 edges overlap.  Then
 //   * lists of at least kLongWords 16-byte words are streamed one at a time by the whole
 //     warp, two words in flight per lane, and counted with one warp reduction;
-//   * the shorter lists, each widened to 16-byte boundaries, form one stream of words;
-//     every round each lane takes one word (a binary search over the batch's prefix sums
-//     names its list), loads it and probes its valid entries, and each edge's owner lane
-//     adds the hits that fell in its list from three ballots of the per-lane counts (0..4).
+//   * the shorter lists, each widened to 32-byte boundaries, form one stream of 8-entry
+//     granules; every round each lane takes one granule (a binary search over the batch's
+//     prefix sums names its list), loads it and probes its valid entries, and each edge's
+//     owner lane adds the hits that fell in its list from four ballots of the per-lane
+//     counts (0..8).
 constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
 constexpr int kWordsInFlight = 2;        // hash kernel (48+ registers would cost occupancy)
 constexpr int kWordsInFlightBitmap = 6;  // bitmap kernel: one CTA per SM, 64 registers at 6 (s22: -0.6 ms against 4)
@@ -272,50 +273,52 @@ __device__ __forceinline__ uint32_t warp_list(const uint32_t* __restrict__ adj, 
     return h;
 }
 
-// The short lists of a batch as one stream of 16-byte words.  Lane i's list covers words
-// [excl_i, incl_i) of the stream; each round every lane takes kShortRounds words (a
-// binary search over the inclusive prefixes names each word's list), issues their loads
-// together, probes the valid entries, and the hits are credited to the owning lanes from
-// three ballots of the per-word counts (0..4).  Returns this lane's own count.
-constexpr int kShortRounds = 1;   // measured: 2 costs more in registers than it gains
+// The short lists of a batch as one stream of granules, kGranuleWords 16-byte words each
+// (8 entries, 32-byte aligned).  Lane i's list covers granules [excl_i, incl_i) of the
+// stream; each round every lane takes one granule (a binary search over the inclusive
+// prefixes names its list), loads its words, probes the valid entries, and the hits are
+// credited to the owning lanes from four ballots of the per-granule counts (0..8).  Returns
+// this lane's own count.  Two words per granule halve the search and the crediting per
+// entry (R-MAT s22: 14.78 -> 14.56 ms over the stage); four words measured no faster (the
+// lists' rounding wastes more), and one granule of two separate rounds costs more registers.
+constexpr uint32_t kGranuleWords = 2;
+constexpr uint32_t kGranuleEntries = 4u * kGranuleWords;   // adjacency arrays carry this many entries of padding
 
 template <typename Probe>
-__device__ __forceinline__ uint32_t short_stream(const uint32_t* __restrict__ adj, uint32_t lane, uint32_t wa,
+__device__ __forceinline__ uint32_t short_stream(const uint32_t* __restrict__ adj, uint32_t lane, uint32_t ga,
                                                  uint32_t ub, uint32_t ue, uint32_t incl, uint32_t excl,
                                                  uint32_t total, Probe probe) {
+    constexpr int kHitBits = 4;   // hits per granule <= 8
     uint32_t cnt = 0;
-    for (uint32_t base = 0; base < total; base += 32u * kShortRounds) {
-        uint4 x[kShortRounds];
-        uint32_t pw[kShortRounds], lbw[kShortRounds], lew[kShortRounds];
+    for (uint32_t y0 = 0; y0 < total; y0 += 32u) {
+        const uint32_t y = y0 + lane;
+        uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
 #pragma unroll
-        for (int r = 0; r < kShortRounds; ++r) {
-            const uint32_t y = base + 32u * r + lane;
-            uint32_t j = 0;   // owner: first lane whose inclusive prefix exceeds y
-#pragma unroll
-            for (int st = 16; st > 0; st >>= 1) {
-                const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + st - 1);
-                if (pj <= y) j += st;
-            }
-            j &= 31u;
-            const uint32_t aj = __shfl_sync(0xFFFFFFFFu, wa, j);
-            const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
-            lbw[r] = __shfl_sync(0xFFFFFFFFu, ub, j);
-            lew[r] = __shfl_sync(0xFFFFFFFFu, ue, j);
-            pw[r] = aj + 4u * (y - ej);
-            x[r] = y < total ? __ldg(reinterpret_cast<const uint4*>(adj + pw[r])) : make_uint4(0, 0, 0, 0);
+        for (int st = 16; st > 0; st >>= 1) {
+            const uint32_t pj = __shfl_sync(0xFFFFFFFFu, incl, j + st - 1);
+            if (pj <= y) j += st;
         }
+        j &= 31u;
+        const uint32_t aj = __shfl_sync(0xFFFFFFFFu, ga, j);
+        const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
+        const uint32_t lb = __shfl_sync(0xFFFFFFFFu, ub, j);
+        const uint32_t le = __shfl_sync(0xFFFFFFFFu, ue, j);
+        const uint32_t p = aj + kGranuleEntries * (y - ej);
+        uint32_t h = 0;
+        if (y < total) {
+            uint4 x[kGranuleWords];
 #pragma unroll
-        for (int r = 0; r < kShortRounds; ++r) {
-            const uint32_t y0 = base + 32u * r;
-            const uint32_t h = (y0 + lane < total) ? probe(x[r], pw[r], lbw[r], lew[r]) : 0u;
-            const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, h & 1u);
-            const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, h & 2u);
-            const uint32_t b2 = __ballot_sync(0xFFFFFFFFu, h & 4u);
-            const int lo = (int)min(max((int64_t)excl - (int64_t)y0, (int64_t)0), (int64_t)32);
-            const int hi = (int)min(max((int64_t)incl - (int64_t)y0, (int64_t)0), (int64_t)32);
-            const uint32_t m = lane_range_mask(lo, hi);
-            cnt += __popc(b0 & m) + 2u * __popc(b1 & m) + 4u * __popc(b2 & m);
+            for (uint32_t q = 0; q < kGranuleWords; ++q) x[q] = __ldg(reinterpret_cast<const uint4*>(adj + p + 4u * q));
+#pragma unroll
+            for (uint32_t q = 0; q < kGranuleWords; ++q) h += probe(x[q], p + 4u * q, lb, le);
         }
+        // this lane's granules within the round (stream positions below 2^31)
+        const int lo = min(max((int)excl - (int)y0, 0), 32);
+        const int hi = min(max((int)incl - (int)y0, 0), 32);
+        const uint32_t m = lane_range_mask(lo, hi);
+#pragma unroll
+        for (int bit = 0; bit < kHitBits; ++bit)
+            cnt += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, (h >> bit) & 1u) & m) << bit;
     }
     return cnt;
 }
@@ -348,8 +351,9 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
     uint32_t cur = ub;
     if (done_long) end = ub;
     for (;;) {
-        const uint32_t wa = cur & ~3u;
-        const uint32_t sw = end > cur ? (((end + 3u) & ~3u) - wa) >> 2 : 0u;
+        const uint32_t ga = cur & ~(kGranuleEntries - 1u);
+        const uint32_t sw = end > cur ? (((end + kGranuleEntries - 1u) & ~(kGranuleEntries - 1u)) - ga) / kGranuleEntries
+                                      : 0u;
         if (__ballot_sync(0xFFFFFFFFu, sw != 0) == 0) break;
         uint32_t incl = sw;
 #pragma unroll
@@ -359,8 +363,8 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
         }
         const uint32_t excl = incl - sw;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        words += total;
-        cnt += short_stream(adj, lane, wa, cur, end, incl, excl, total, probe);
+        words += total * kGranuleWords;
+        cnt += short_stream(adj, lane, ga, cur, end, incl, excl, total, probe);
         // the next phase: what the hits found so far require (at least 8 words more)
         const uint32_t need = needed_entries(du, tlo, cnt);
         const uint32_t next = (!done_long && ub + need > end) ? min(ue, max(ub + need, end + 32u)) : end;
@@ -376,7 +380,7 @@ __device__ __forceinline__ uint32_t count_batch(const uint32_t* __restrict__ adj
 //   * kSmallSerial: the pivot's list in a per-warp hash table; the warp counts the lists one
 //     at a time, lanes over a list, one warp reduction per list;
 //   * kSmallBatched: the same table; the 32 lists are streamed together by count_batch (one
-//     stream of 16-byte words, hits credited by ballot and popc), with the early stop of a
+//     stream of 8-entry granules, hits credited by ballot and popc), with the early stop of a
 //     one-shot run.  The loads of different lists overlap: it pays where most edges are
 //     counted (dense graphs), and costs where the degree prune leaves few;
 //   * kSmallSearch: as kSmallBatched, but the pivot's list is kept sorted and each entry is

@@ -83,7 +83,9 @@ typedef struct scan_stats {
     double ms_total;            /* first event to last event of the run                       */
     double ms_cn_kernel[5];     /* similarity-stage kernels: small pivots; the three hash-table
                                    classes (1024 / 4096 / chunk entries); the hubs (mid hubs
-                                   and larger hubs together)                                   */
+                                   and larger hubs together).  The hubs run on a second stream
+                                   beside the others, so these intervals overlap: each is its
+                                   kernel's span on its own stream                             */
     uint64_t cn_work_items[5];  /* pivots (small class) or tasks (the others) of each           */
     uint32_t kernel_launches;   /* kernels this library launched for the run                  */
     uint32_t reserved;
