@@ -36,6 +36,7 @@ kernels (its cubin, its launch order) are timed on the same graph as a context f
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -559,6 +560,10 @@ def main():
     e2e_value, e2e_s, e2e_matches, e2e_step_ms, e2e_cold_ms, e2e_out = None, 0.0, None, [], [], None
     if args.e2e_steps > 0:
         sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)   # warm
+        # Python's cyclic collector stays off while the calls are timed, as timeit does: a
+        # full collection over torch's and numpy's objects once stalled one call by ~30 ms
+        gc.collect()
+        gc.disable()
         dist.barrier()
         t = time.perf_counter()
         for _ in range(args.e2e_steps):
@@ -566,6 +571,7 @@ def main():
             out = sg.GPUScan(h_off, h_adj, float(args.eps), args.mu)
             e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
         e2e_s = dist.max(time.perf_counter() - t)
+        gc.enable()
         e2e_value = world * E * args.e2e_steps / e2e_s
         check = g.run(args.eps, args.mu, sg.PRED_REF_F64, device=local).label
         e2e_matches = bool(np.array_equal(out, check))
@@ -635,6 +641,7 @@ def main():
                     "ms_per_step": e2e_s / max(args.e2e_steps, 1) * 1e3,
                     "step_ms": [round(x, 3) for x in e2e_step_ms], "labels_match_resident_run": e2e_matches,
                     "cold_cache_step_ms": [round(x, 3) for x in e2e_cold_ms],
+                    "python_gc": "collected before the timed calls and disabled during them (as timeit does)",
                     "buffers": "steps reuse the library's cache of freed device buffers (default limit 8 GiB); "
                                "cold_cache_step_ms: the same call after the cache was emptied"},
             "roofline": roof,

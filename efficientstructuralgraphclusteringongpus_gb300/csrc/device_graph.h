@@ -64,6 +64,7 @@ struct DeviceGraph {
     unsigned long long* work = nullptr;
     unsigned long long* cn_ctr = nullptr;
     uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel
+    uint32_t* np_tab = nullptr;            // launch_cn: prune thresholds of pivot degrees < kPruneTable
     bool has_split = false;                // the plan splits some pivot into chunks
     float* tau = nullptr;                  // served graphs: 2E similarity thresholds (k_tau)   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;

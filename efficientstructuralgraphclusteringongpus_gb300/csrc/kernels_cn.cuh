@@ -9,7 +9,10 @@
 //      copy (one-shot runs, k_cn_filter), a bucketed hash table (full counts, k_cn_big) or
 //      a bitmap of hot ids (hubs, k_cn_bitmap);
 //   2. warps stream the lower endpoints' lists N(u) with 16-byte loads and probe each
-//      element against it; ballots and warp reductions give the counts.
+//      element against it; ballots and warp reductions give the counts;
+//   3. in one-shot runs the degree prune, the early stop and the predicate skip use integer
+//      and float thresholds per pivot (predicate.cuh: pivot_tests, count_floor); only a
+//      count that may be similar takes the two predicates in double and 128-bit integers.
 // Per edge this reads deg(u) <= deg(v) entries, the shorter list, once; the longer
 // list is read once per task, not once per edge.
 //
@@ -125,6 +128,9 @@ struct CnPrune {
     // null for a single graph
     const PredParams* gpp;
     const uint32_t* vgid;
+    double pq2;          // PredParams::pq2, eps2_floor (see pred_derive)
+    float eps2_floor;
+    const uint32_t* np_tab;   // single-graph runs: pivot_tests(d).np for d < kPruneTable (k_prune_table)
 };
 
 // The parameters for pivot v in a batched run: eps and the predicate of v's graph (the
@@ -138,7 +144,34 @@ __device__ __forceinline__ CnPrune prune_of_graph(const CnPrune& pr, uint32_t v)
     r.p = g.p;
     r.q = g.q;
     r.mode = g.mode;
+    r.pq2 = g.pq2;
+    r.eps2_floor = g.eps2_floor;
     return r;
+}
+
+// Per-pivot constants of the per-edge tests (predicate.cuh) for pivot degree dv.  The prune
+// threshold of a degree below kPruneTable comes from a table filled once per run: its
+// double arithmetic (about ten FP64 instructions, 16 issue cycles each per warp on this
+// part) would otherwise be paid by every small pivot, most of which have few lower edges.
+constexpr uint32_t kPruneTable = 4096;
+
+__device__ __forceinline__ PivotTests pivot_tests(uint32_t dv, const CnPrune& P) {
+    if (P.np_tab && dv < kPruneTable) {
+        PivotTests t;
+        t.np = P.np_tab[dv];
+        t.tscale = P.eps2_floor * (float)(dv + 1ull);
+        return t;
+    }
+    return pivot_tests(dv, P.on != 0, P.eps, P.p, P.q, P.pq2, P.eps2_floor);
+}
+
+// np_tab[d] = pivot_tests(d).np for every d < kPruneTable (capped at 2^32 - 1, above every
+// du + 1 of a graph with fewer than 2^32 - 16 adjacency entries).
+__global__ void k_prune_table(CnPrune pr, uint32_t* __restrict__ np_tab) {
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= kPruneTable) return;
+    const PivotTests t = pivot_tests(d, pr.on != 0, pr.eps, pr.p, pr.q, pr.pq2, pr.eps2_floor);
+    np_tab[d] = t.np > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)t.np;
 }
 
 // Predicate fused into the counting kernels of a one-shot run whose plan splits no pivot:
@@ -153,19 +186,24 @@ struct FusedPred {
 };
 
 // Warp-wide (holds a ballot): every lane calls it; lanes with valid set test edge k
-// {u lower, v pivot} with count t.  v is the same for every lane of the call.
-__device__ __forceinline__ void fused_predicate(const FusedPred& fp, const CnPrune& pr, bool valid, uint32_t k,
-                                                uint32_t u, uint32_t v, uint32_t du, uint32_t dv, uint32_t t,
-                                                uint32_t lane, unsigned long long& nsim, unsigned long long& ndis) {
+// {u lower, v pivot} with count t.  v is the same for every lane of the call.  decided: both
+// predicates reject the edge (pruned, or t below count_floor), so neither is evaluated.
+// sim starts zeroed, so only similar edges are written.
+__device__ __forceinline__ void fused_predicate(const FusedPred& fp, const CnPrune& pr, bool valid, bool decided,
+                                                uint32_t k, uint32_t u, uint32_t v, uint32_t du, uint32_t dv,
+                                                uint32_t t, uint32_t lane, unsigned long long& nsim,
+                                                unsigned long long& ndis) {
     bool s = false;
-    if (valid) {
+    if (valid && !decided) {
         const bool r = ref_f64_similar(t, du, dv, pr.eps);
         const bool x = exact_similar(t, du, dv, pr.p, pr.q);
         s = pr.mode ? r : x;
         ndis += (r != x);
         nsim += s;
-        fp.sim[k] = s;
-        if (s) atomicAdd(&fp.sd[u], 1);
+        if (s) {
+            fp.sim[k] = 1;
+            atomicAdd(&fp.sd[u], 1);
+        }
     }
     const uint32_t nv = __popc(__ballot_sync(0xFFFFFFFFu, s));
     if (lane == 0 && nv) atomicAdd(&fp.sd[v], (int32_t)nv);
@@ -183,18 +221,6 @@ __device__ __forceinline__ void fused_totals(const FusedPred& fp, uint32_t lane,
         if (nsim) atomicAdd(&fp.ctr->similar_edges, nsim);
         if (ndis) atomicAdd(&fp.ctr->disagreements, ndis);
     }
-}
-
-__device__ __forceinline__ bool cn_pruned(uint32_t du, uint32_t dv, const CnPrune& pr) {
-    return pr.on && ref_f64_never(du, dv, pr.eps) && exact_never(du, dv, pr.p, pr.q);
-}
-
-// Early-stop threshold of an unpruned edge in a one-shot run: the least count either
-// predicate could accept.  0 (count everything) when the reference's int square of the
-// count could wrap (du + 1 > 46340, where its test is not monotone in the count).
-__device__ __forceinline__ uint32_t min_similar_count(uint32_t du, uint32_t dv, const CnPrune& pr) {
-    if (du + 1u > 46340u) return 0u;
-    return min(exact_min_count(du, dv, pr.p, pr.q), ref_min_count(du, dv, pr.eps));
 }
 
 // First position in adj[b, e) whose value is >= key (scalar, uniform across the warp).
@@ -440,6 +466,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
         if constexpr (kPerGraph) Pg = prune_of_graph(pr, v);
         const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t b = off[v], e = off[v + 1];
+        const PivotTests pt = pivot_tests(e - b, P);
         if constexpr (kStrategy == kSmallSearch) {
             for (uint32_t j = b + lane; j < e; j += 32) tab[j - b] = adj[j];   // sorted copy (e - b <= 128)
         } else {
@@ -455,15 +482,17 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
             const uint32_t kk = kb + lane;
             const bool vk = kk < k1;
             uint32_t u = 0, ub = 0, ue = 0, du = 0, mc = 0;
+            bool pruned = false;
             if (vk) {
                 u = lo_adj[kk];
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, e - b, P)) ue = ub;   // cn stays 0
+                pruned = edge_pruned(du, pt);
+                if (pruned) ue = ub;   // cn stays 0
             }
             if constexpr (kStrategy != kSmallSerial) {
-                const uint32_t tlo = (P.on && ue > ub) ? min_similar_count(du, e - b, P) : 0u;
+                const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, pt) : 0u;
                 mc = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                  [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
                                                      if constexpr (kStrategy == kSmallSearch)
@@ -486,7 +515,9 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
                 }
             }
             if (vk) cn[kk] = mc;
-            if (fp.sim) fused_predicate(fp, P, vk, kk, u, v, du, e - b, mc, lane, nsim, ndis);
+            if (fp.sim)
+                fused_predicate(fp, P, vk, pruned || mc < count_floor(du, pt), kk, u, v, du, e - b, mc, lane, nsim,
+                                ndis);
         }
         if (lane == 0 && counted) {
             atomicAdd(&ctr[0], (unsigned long long)words);
@@ -510,12 +541,11 @@ __device__ __forceinline__ uint32_t next_task(uint32_t* queue, uint32_t prev, bo
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap, uint32_t* queue,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
-                         CnPrune pr, unsigned long long* __restrict__ ctr, FusedPred fp) {
+                         CnPrune pr, unsigned long long* __restrict__ ctr) {
     extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nb = cap / 4;
-    unsigned long long nsim = 0, ndis = 0;
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
         const CnTask tk = tasks[t];
@@ -526,6 +556,7 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
         for (uint32_t j = tk.cb + threadIdx.x; j < tk.ce; j += blockDim.x) bucket_insert(tab, nb, adj[j]);
         __syncthreads();
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
+        const PivotTests pt = pivot_tests(ve - vb, pr);   // np = 0 when counting in full
         const uint32_t lo_id = (tk.cb > vb) ? adj[tk.cb] : 0u;          // chunk id range
         const uint32_t hi_id = (tk.ce < ve) ? adj[tk.ce - 1] : kEmpty;
         for (;;) {
@@ -542,14 +573,14 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, ve - vb, pr)) ue = ub;
+                if (edge_pruned(du, pt)) ue = ub;
                 counted = ue > ub && tk.cb == vb;               // once per edge: in its first chunk
                 if (tk.chunked && ue > ub) {
                     if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
                     if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
                 }
             }
-            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? min_similar_count(ue - ub, ve - vb, pr) : 0u;
+            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? count_floor(du, pt) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                              [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
@@ -564,11 +595,9 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 if (!tk.chunked) cn[k] = cnt;
                 else if (cnt) atomicAdd(&cn[k], cnt);           // cn was zeroed before the launch
             }
-            if (fp.sim) fused_predicate(fp, pr, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
         }
         __syncthreads();
     }
-    fused_totals(fp, lane, nsim, ndis);
 }
 
 // One-shot runs on the hash classes (no split pivot, predicate fused): nearly every counted
@@ -672,6 +701,7 @@ __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks,
         if constexpr (kPerGraph) Pg = prune_of_graph(pr, tk.v);
         const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1], dv = ve - vb;   // dv <= list_entries (no split)
+        const PivotTests pt = pivot_tests(dv, P);
         for (uint32_t i = threadIdx.x; i < nwords / 4; i += blockDim.x)
             reinterpret_cast<uint4*>(bits)[i] = make_uint4(0, 0, 0, 0);
         if (threadIdx.x == 0) next_batch = 0;
@@ -692,13 +722,15 @@ __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks,
             const uint32_t k = strided ? tk.e0 + j + lane * nbatch : tk.e0 + 32u * j + lane;
             const bool valid = k < tk.e1;
             uint32_t ub = 0, ue = 0, u = 0, du = 0, tlo = 0;
+            bool pruned = false;
             if (valid) {
                 u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, dv, P)) ue = ub;
-                if (ue > ub) tlo = min_similar_count(du, dv, P);
+                pruned = edge_pruned(du, pt);
+                if (pruned) ue = ub;
+                if (ue > ub) tlo = count_floor(du, pt);
             }
             // tlo = 0: any count may be similar, so the bound decides nothing; count exactly
             const bool bound_scan = ue > ub && tlo > 0;
@@ -722,7 +754,7 @@ __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks,
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
-            fused_predicate(fp, P, valid, k, u, tk.v, du, dv, cnt, lane, nsim, ndis);
+            fused_predicate(fp, P, valid, pruned || cnt < tlo, k, u, tk.v, du, dv, cnt, lane, nsim, ndis);
         }
         __syncthreads();
     }
@@ -795,6 +827,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
         if constexpr (kPerGraph) Pg = prune_of_graph(pr, tk.v);
         const CnPrune& P = kPerGraph ? Pg : pr;
         const uint32_t vb = off[tk.v], ve = off[tk.v + 1];
+        const PivotTests pt = pivot_tests(ve - vb, P);
         uint32_t ntb = 8;                                // tail buckets: >= tail size (load <= 1/4),
         while (ntb < tk.cb) ntb <<= 1;                   // capped at the table (load <= 1/2 there)
         ntb = min(ntb, kTailSlots / 4);
@@ -819,14 +852,16 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
             const uint32_t k = strided ? tk.e0 + j + lane * nbatch : tk.e0 + 32u * j + lane;
             const bool valid = k < tk.e1;
             uint32_t ub = 0, ue = 0, u = 0, du = 0;
+            bool pruned = false;
             if (valid) {
                 u = lo_adj[k];
                 ub = off[u];
                 ue = off[u + 1];
                 du = ue - ub;
-                if (cn_pruned(du, ve - vb, P)) ue = ub;
+                pruned = edge_pruned(du, pt);
+                if (pruned) ue = ub;
             }
-            const uint32_t tlo = (P.on && ue > ub) ? min_similar_count(ue - ub, ve - vb, P) : 0u;
+            const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, pt) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlightBitmap>(radj, lane, ub, ue, tlo, long_words, words,
                                                                    [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
@@ -839,7 +874,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) cn[k] = cnt;
-            if (fp.sim) fused_predicate(fp, P, valid, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
+            if (fp.sim) fused_predicate(fp, P, valid, pruned || cnt < tlo, k, u, tk.v, du, ve - vb, cnt, lane, nsim, ndis);
         }
         __syncthreads();
         for (uint32_t j = vb + threadIdx.x; j < ve; j += blockDim.x) {   // clear this pivot's bits

@@ -89,10 +89,78 @@ __host__ __device__ inline uint32_t ref_min_count(uint32_t du, uint32_t dv, doub
     return a > 46340 ? kNoCount : a - 2;
 }
 
+// Per-pivot constants of a one-shot run's per-edge tests.  GB300 issues double arithmetic at
+// a small fraction of its integer and float rate: with every edge taking the prune, the
+// early-stop threshold (a double square root) and both predicates in double, the FP64 pipe
+// was 74% busy in the 1,024-entry class.  So each pivot's 'never' tests are reduced once to
+// an integer threshold on du, the early-stop threshold is a float lower bound, and an edge
+// takes the double tests only when the count can still be similar.
+struct PivotTests {
+    uint64_t np;     // the edge is pruned (both predicates' 'never' test holds) iff du + 1 < np
+    float tscale;    // eps2_floor * (dv + 1), for count_floor
+};
+
+__host__ __device__ inline PivotTests pivot_tests(uint32_t dv, bool on, double eps, uint64_t p, uint64_t q,
+                                                double pq2, float eps2_floor) {
+    constexpr uint64_t kAll = 1ull << 33;      // above every du + 1
+    const uint64_t dv1 = dv + 1ull;
+    PivotTests t;
+    t.tscale = eps2_floor * (float)dv1;
+    t.np = 0;
+    if (!on) return t;
+    // ref-f64 'never', (double)du1 < dv1 * eps * eps: true exactly below ceil(dv1 * eps * eps)
+    const double rn = (double)dv1 * eps * eps;
+    const uint64_t n_ref = !(rn > 0.0) ? 0ull : rn >= (double)kAll ? kAll : (uint64_t)ceil(rn);
+    // exact 'never', q^2 du1 < p^2 dv1: true exactly below ceil(p^2 dv1 / q^2); the double
+    // estimate is within one of it (relative error < 2^-50 on a value below 2^33)
+    uint64_t n_ex = kAll;
+    if (p <= q) {
+        const unsigned __int128 num = (unsigned __int128)(p * p) * dv1;
+        const uint64_t q2 = q * q;
+        const double est = pq2 * (double)dv1;
+        uint64_t c = !(est > 0.0) ? 0ull : est >= (double)kAll ? kAll : (uint64_t)est;
+        for (int i = 0; i < 4 && c > 0 && (unsigned __int128)q2 * (c - 1) >= num; ++i) --c;
+        for (int i = 0; i < 4 && c < kAll && (unsigned __int128)q2 * c < num; ++i) ++c;
+        const bool ok = (unsigned __int128)q2 * c >= num && (c == 0 || (unsigned __int128)q2 * (c - 1) < num);
+        if (!ok) return t;                     // cannot happen; prune nothing rather than guess
+        n_ex = c;
+    }
+    t.np = n_ref < n_ex ? n_ref : n_ex;
+    return t;
+}
+
+__host__ __device__ __forceinline__ bool edge_pruned(uint32_t du, const PivotTests& pt) { return du + 1ull < pt.np; }
+
+// A lower bound of the least count either predicate accepts (exact_min_count and
+// ref_min_count): floor(sqrt(eps2_floor (du+1)(dv+1)) (1 - 1e-6)) - 2.  The float roundings
+// (eps2_floor, two products, the square root, the scaling) stay below 4e-7 relative, and the
+// reference's double threshold is at least eps^2 (du+1)(dv+1)(1 - 2^-51), so every count
+// below the bound is rejected by both.  0 where the reference's int square of the count can
+// wrap (du + 1 > 46340: its test is not monotone there) and where any count may be similar.
+__host__ __device__ __forceinline__ uint32_t count_floor(uint32_t du, const PivotTests& pt) {
+    if (du + 1u > 46340u) return 0u;
+    const float s = sqrtf(pt.tscale * (float)(du + 1u)) * 0.999999f;
+    const int l = (int)s - 2;
+    return l > 0 ? (uint32_t)l : 0u;
+}
+
 struct PredParams {
     double eps;          // ref-f64 value (strtod of the decimal text, like atof in main.cpp:26)
     uint64_t p, q;       // exact value p/q
     int mode;            // 0 exact, 1 ref-f64
+    // derived by pred_derive from the three above:
+    double pq2;          // p^2 / q^2 rounded (an estimate only; infinity when p > q)
+    float eps2_floor;    // min(p^2/q^2, eps*eps) as a float: within 2^-24 of a lower bound
+                         // on the eps^2 of both predicates (count_floor's margin covers it)
 };
+
+// Fill the derived fields; call after eps, p or q change.
+inline void pred_derive(PredParams* pp) {
+    pp->pq2 = pp->p > pp->q ? INFINITY : ((double)pp->p * (double)pp->p) / ((double)pp->q * (double)pp->q);
+    const double e2 = pp->eps * pp->eps;
+    double m = pp->pq2 < e2 ? pp->pq2 : e2;
+    if (!(m > 0.0)) m = 0.0;                 // eps = 0 (or not a number): no early stop
+    pp->eps2_floor = m > 3.0e38 ? 3.0e38f : (float)m;
+}
 
 }  // namespace scan

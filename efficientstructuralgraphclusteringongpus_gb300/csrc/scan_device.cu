@@ -536,6 +536,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     SCAN_TRY(dalloc(d.get(), &d->cn, d->E));
     SCAN_TRY(dalloc(d.get(), &d->cn_ctr, 2));
     SCAN_TRY(dalloc(d.get(), &d->task_queue, 8));
+    SCAN_TRY(dalloc(d.get(), &d->np_tab, kPruneTable));
     uint8_t* rs_mem = nullptr;
     SCAN_TRY(dalloc(d.get(), &rs_mem, run_scratch_bytes(d->n, d->E)));
     run_scratch_bind(&d->rs, rs_mem, d->n, d->E);
@@ -660,7 +661,7 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
                 k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
                                                                 d->task_queue + c, d->off,
                                                                 d->adj, d->lo_adj, d->cn, d->long_words, pr,
-                                                                d->cn_ctr, fp);
+                                                                d->cn_ctr);
             }
             ++*launches;
         }
@@ -692,8 +693,9 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
 scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prune, const RunScratch* fused,
                       const BatchParams* bp) {
     if (d->device < 0 || d->device >= 64) return fail(SCAN_ERR_INVALID_ARG, "device index must be < 64");
-    CnPrune pr{0.0, 0, 1, 0u, 0, nullptr, nullptr};
-    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u, prune->mode, nullptr, nullptr};
+    CnPrune pr{0.0, 0, 1, 0u, 0, nullptr, nullptr, 0.0, 0.f, nullptr};
+    if (prune) pr = CnPrune{prune->eps, prune->p, prune->q, 1u, prune->mode, nullptr, nullptr, prune->pq2,
+                            prune->eps2_floor, nullptr};
     const bool per_graph = prune && bp;
     if (per_graph) {
         pr.gpp = bp->gpp;
@@ -706,6 +708,11 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
     SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
+    if (prune && !per_graph) {   // batches: each pivot's graph has its own eps
+        k_prune_table<<<kPruneTable / 256, 256, 0, s>>>(pr, d->np_tab);
+        pr.np_tab = d->np_tab;
+        ++*launches;
+    }
     return per_graph ? launch_cn_impl<true>(d, launches, pr, fp) : launch_cn_impl<false>(d, launches, pr, fp);
 }
 
@@ -849,6 +856,7 @@ scan_status make_pred(const char* eps_decimal, PredParams* pp, scan_predicate mo
     pp->q = q;
     pp->mode = mode == SCAN_PRED_REF_F64 ? 1 : 0;
     if (pp->p > pp->q) { pp->p = 1; pp->q = 0; }   // eps > 1: exact predicate is never true
+    pred_derive(pp);
     return SCAN_OK;
 }
 
@@ -1163,6 +1171,7 @@ int32_t* scan_gpuscan_compat(int64_t n, int64_t m, const int32_t* adj, const uin
     PredParams pp;
     if (make_pred(text, &pp, SCAN_PRED_REF_F64) != SCAN_OK) return nullptr;
     pp.eps = eps;   // the double itself, exactly as the caller computed it
+    pred_derive(&pp);
     const size_t bytes = (size_t)n * sizeof(int32_t);
     int32_t* out = static_cast<int32_t*>(std::malloc(bytes));
     if (!out) {
