@@ -477,7 +477,10 @@ def chung_lu_bench(args, device: int, runs_resident: int, runs_streamed: int) ->
         st = runs[-1].stats
         out[tag] = {"ms_per_step": float(np.mean(ms)), "edges_per_s": g.num_edges / (float(np.mean(ms)) / 1e3),
                     "ms_similarity": st["ms_similarity"], "cores": st["num_cores"], "clusters": st["num_clusters"],
-                    "similar_edges": st["num_similar_edges"], "device_bytes": g.device_bytes}
+                    "similar_edges": st["num_similar_edges"], "device_bytes": g.device_bytes,
+                    # each kernel's span on its stream (small pivots, three hash classes, hubs)
+                    "ms_cn_kernel": [round(float(x), 3) for x in st["ms_cn_kernel"]],
+                    "cn_work_items": [int(x) for x in st["cn_work_items"]], "cn_words": int(st["cn_words"])}
         return runs[-1].label
 
     t = time.perf_counter()

@@ -32,6 +32,10 @@ struct scan_batch {
     uint32_t* vgid = nullptr;            // device, n
     PredParams* gpp = nullptr;           // device, count
     int32_t* gmu = nullptr;              // device, count
+    PredParams* sets = nullptr;          // device, kPruneSets: distinct parameter sets of a run
+    uint32_t* nsets = nullptr;           // device
+    uint32_t* np_tabs = nullptr;         // device, kPruneSets * kPruneTable prune thresholds
+    PredParams* h_sets = nullptr;        // pinned, kPruneSets + 1 (the last: the count)
     PredParams* h_gpp = nullptr;         // pinned, count
     int32_t* h_gmu = nullptr;            // pinned, count
     int32_t* h_label = nullptr;          // pinned, n
@@ -54,6 +58,9 @@ void batch_free_device(scan_batch* b) {
     if (b->vgid) cudaFree(b->vgid);
     if (b->gpp) cudaFree(b->gpp);
     if (b->gmu) cudaFree(b->gmu);
+    for (void* p : {(void*)b->sets, (void*)b->nsets, (void*)b->np_tabs})
+        if (p) cudaFree(p);
+    if (b->h_sets) cudaFreeHost(b->h_sets);
     for (void* p : {(void*)b->h_gpp, (void*)b->h_gmu, (void*)b->h_label, (void*)b->h_role, (void*)b->h_ctr,
                     (void*)b->h_flag})
         if (p) cudaFreeHost(p);
@@ -115,6 +122,10 @@ scan_status scan_batch_create(const scan_graph* const* graphs, uint32_t count, i
     B_CUDA(cudaMalloc(&b->vgid, N * sizeof(uint32_t)));
     B_CUDA(cudaMalloc(&b->gpp, count * sizeof(PredParams)));
     B_CUDA(cudaMalloc(&b->gmu, count * sizeof(int32_t)));
+    B_CUDA(cudaMalloc(&b->sets, kPruneSets * sizeof(PredParams)));
+    B_CUDA(cudaMalloc(&b->nsets, sizeof(uint32_t)));
+    B_CUDA(cudaMalloc(&b->np_tabs, (size_t)kPruneSets * kPruneTable * sizeof(uint32_t)));
+    B_CUDA(cudaHostAlloc(&b->h_sets, (kPruneSets + 1) * sizeof(PredParams), cudaHostAllocDefault));
     B_CUDA(cudaMemcpy(b->vgid, vgid.data(), N * sizeof(uint32_t), cudaMemcpyHostToDevice));
     B_CUDA(cudaHostAlloc(&b->h_gpp, count * sizeof(PredParams), cudaHostAllocDefault));
     B_CUDA(cudaHostAlloc(&b->h_gmu, count * sizeof(int32_t), cudaHostAllocDefault));
@@ -145,13 +156,34 @@ scan_status scan_batch_run(scan_batch* b, const char* const* eps_decimal, const 
         b->h_gmu[i] = mu[i];
         if (!out_labels[i]) return fail(SCAN_ERR_INVALID_ARG, "null output for graph " + std::to_string(i));
     }
+    // Distinct (eps, p, q) sets: each gets a prune-threshold table (the predicate mode does
+    // not enter the thresholds); graphs past kPruneSets sets compute them per pivot.
+    uint32_t nsets = 0;
+    for (uint32_t i = 0; i < b->count; ++i) {
+        PredParams& g = b->h_gpp[i];
+        g.np_set = 0xFFFFFFFFu;
+        for (uint32_t k = 0; k < nsets; ++k) {
+            const PredParams& r = b->h_sets[k];
+            if (std::memcmp(&r.eps, &g.eps, sizeof(double)) == 0 && r.p == g.p && r.q == g.q) {
+                g.np_set = k;
+                break;
+            }
+        }
+        if (g.np_set == 0xFFFFFFFFu && nsets < kPruneSets) {
+            b->h_sets[nsets] = g;
+            g.np_set = nsets++;
+        }
+    }
+    std::memcpy(&b->h_sets[kPruneSets], &nsets, sizeof(nsets));
     DeviceGraph* d = b->d;
     std::lock_guard<std::mutex> lock(d->mu);
     B_CUDA(cudaSetDevice(b->device));
     cudaStream_t s = d->stream;
     B_CUDA(cudaMemcpyAsync(b->gpp, b->h_gpp, b->count * sizeof(PredParams), cudaMemcpyHostToDevice, s));
     B_CUDA(cudaMemcpyAsync(b->gmu, b->h_gmu, b->count * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    BatchParams bp{b->vgid, b->gpp, b->gmu};
+    B_CUDA(cudaMemcpyAsync(b->sets, b->h_sets, kPruneSets * sizeof(PredParams), cudaMemcpyHostToDevice, s));
+    B_CUDA(cudaMemcpyAsync(b->nsets, &b->h_sets[kPruneSets], sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    BatchParams bp{b->vgid, b->gpp, b->gmu, b->sets, b->nsets, b->np_tabs};
     PredParams unused{};
     // The pass: with no split pivot, the one-shot path of a single run (degree prune, early
     // stop, the filter kernels, predicate fused into the counting), each pivot taking eps and

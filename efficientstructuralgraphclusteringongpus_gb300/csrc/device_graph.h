@@ -133,6 +133,11 @@ struct BatchParams {
     const uint32_t* vgid;
     const PredParams* gpp;
     const int32_t* gmu;
+    // prune-threshold tables: the distinct parameter sets (gpp[i].np_set indexes them; sets
+    // beyond kPruneSets compute their thresholds per pivot), their number, the tables
+    const PredParams* sets;
+    const uint32_t* nsets;
+    uint32_t* np_tabs;
 };
 
 // predicate -> cores -> union-find -> attach -> classify from d->cn into r, on stream s.

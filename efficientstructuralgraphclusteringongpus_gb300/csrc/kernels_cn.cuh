@@ -146,14 +146,10 @@ __device__ __forceinline__ CnPrune prune_of_graph(const CnPrune& pr, uint32_t v)
     r.mode = g.mode;
     r.pq2 = g.pq2;
     r.eps2_floor = g.eps2_floor;
+    r.np_tab = pr.np_tab && g.np_set < kPruneSets ? pr.np_tab + (size_t)g.np_set * kPruneTable : nullptr;
     return r;
 }
 
-// Per-pivot constants of the per-edge tests (predicate.cuh) for pivot degree dv.  The prune
-// threshold of a degree below kPruneTable comes from a table filled once per run: its
-// double arithmetic (about ten FP64 instructions, 16 issue cycles each per warp on this
-// part) would otherwise be paid by every small pivot, most of which have few lower edges.
-constexpr uint32_t kPruneTable = 4096;
 
 __device__ __forceinline__ PivotTests pivot_tests(uint32_t dv, const CnPrune& P) {
     if (P.np_tab && dv < kPruneTable) {
@@ -167,11 +163,24 @@ __device__ __forceinline__ PivotTests pivot_tests(uint32_t dv, const CnPrune& P)
 
 // np_tab[d] = pivot_tests(d).np for every d < kPruneTable (capped at 2^32 - 1, above every
 // du + 1 of a graph with fewer than 2^32 - 16 adjacency entries).
+__device__ __forceinline__ uint32_t prune_threshold(uint32_t d, bool on, double eps, uint64_t p, uint64_t q,
+                                                    double pq2) {
+    const PivotTests t = pivot_tests(d, on, eps, p, q, pq2, 0.f);
+    return t.np > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)t.np;
+}
+
 __global__ void k_prune_table(CnPrune pr, uint32_t* __restrict__ np_tab) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= kPruneTable) return;
-    const PivotTests t = pivot_tests(d, pr.on != 0, pr.eps, pr.p, pr.q, pr.pq2, pr.eps2_floor);
-    np_tab[d] = t.np > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)t.np;
+    if (d < kPruneTable) np_tab[d] = prune_threshold(d, pr.on != 0, pr.eps, pr.p, pr.q, pr.pq2);
+}
+
+// Batches: table y (blockIdx.y) for parameter set y < *nsets, pruning on.
+__global__ void k_prune_tables(const PredParams* __restrict__ sets, const uint32_t* __restrict__ nsets,
+                               uint32_t* __restrict__ np_tabs) {
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (y >= *nsets || d >= kPruneTable) return;
+    const PredParams g = sets[y];
+    np_tabs[(size_t)y * kPruneTable + d] = prune_threshold(d, true, g.eps, g.p, g.q, g.pq2);
 }
 
 // Predicate fused into the counting kernels of a one-shot run whose plan splits no pivot:
@@ -492,7 +501,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
                 if (pruned) ue = ub;   // cn stays 0
             }
             if constexpr (kStrategy != kSmallSerial) {
-                const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, pt) : 0u;
+                const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, e - b, pt, P.eps) : 0u;
                 mc = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                  [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
                                                      if constexpr (kStrategy == kSmallSearch)
@@ -516,7 +525,7 @@ k_cn_small(const uint32_t* __restrict__ pivots, uint32_t npiv, const uint32_t* _
             }
             if (vk) cn[kk] = mc;
             if (fp.sim)
-                fused_predicate(fp, P, vk, pruned || mc < count_floor(du, pt), kk, u, v, du, e - b, mc, lane, nsim,
+                fused_predicate(fp, P, vk, pruned || mc < count_floor(du, e - b, pt, P.eps), kk, u, v, du, e - b, mc, lane, nsim,
                                 ndis);
         }
         if (lane == 0 && counted) {
@@ -580,7 +589,7 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                     if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
                 }
             }
-            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? count_floor(du, pt) : 0u;
+            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? count_floor(du, ve - vb, pt, pr.eps) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                              [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
@@ -730,7 +739,7 @@ __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks,
                 du = ue - ub;
                 pruned = edge_pruned(du, pt);
                 if (pruned) ue = ub;
-                if (ue > ub) tlo = count_floor(du, pt);
+                if (ue > ub) tlo = count_floor(du, dv, pt, P.eps);
             }
             // tlo = 0: any count may be similar, so the bound decides nothing; count exactly
             const bool bound_scan = ue > ub && tlo > 0;
@@ -861,7 +870,7 @@ k_cn_bitmap(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t* queue, 
                 pruned = edge_pruned(du, pt);
                 if (pruned) ue = ub;
             }
-            const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, pt) : 0u;
+            const uint32_t tlo = (P.on && ue > ub) ? count_floor(du, ve - vb, pt, P.eps) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlightBitmap>(radj, lane, ub, ue, tlo, long_words, words,
                                                                    [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {

@@ -129,19 +129,34 @@ __host__ __device__ inline PivotTests pivot_tests(uint32_t dv, bool on, double e
     return t;
 }
 
+// The kernels take a pivot's prune threshold for a degree below kPruneTable from a table
+// filled once per run (k_prune_table; a batch fills one per distinct parameter set, up to
+// kPruneSets, k_prune_tables): its double arithmetic (about ten FP64 instructions, 16 issue
+// cycles each per warp on GB300) would otherwise be paid by every small pivot, most of
+// which have few lower edges.
+constexpr uint32_t kPruneTable = 4096;
+constexpr uint32_t kPruneSets = 64;
+
 __host__ __device__ __forceinline__ bool edge_pruned(uint32_t du, const PivotTests& pt) { return du + 1ull < pt.np; }
 
 // A lower bound of the least count either predicate accepts (exact_min_count and
 // ref_min_count): floor(sqrt(eps2_floor (du+1)(dv+1)) (1 - 1e-6)) - 2.  The float roundings
 // (eps2_floor, two products, the square root, the scaling) stay below 4e-7 relative, and the
 // reference's double threshold is at least eps^2 (du+1)(dv+1)(1 - 2^-51), so every count
-// below the bound is rejected by both.  0 where the reference's int square of the count can
-// wrap (du + 1 > 46340: its test is not monotone there) and where any count may be similar.
-__host__ __device__ __forceinline__ uint32_t count_floor(uint32_t du, const PivotTests& pt) {
-    if (du + 1u > 46340u) return 0u;
-    const float s = sqrtf(pt.tscale * (float)(du + 1u)) * 0.999999f;
-    const int l = (int)s - 2;
-    return l > 0 ? (uint32_t)l : 0u;
+// below the bound is rejected by both.  0 where any count may be similar.
+// Where the reference's int square of the count can wrap (du + 1 > 46340), its test is not
+// monotone in the count, but only counts above 46338 wrap: the bound is capped at 46339,
+// below which the square is exact.  When the reference's threshold is 2^31 or more, no
+// square, wrapped or not, reaches it, and the bound is left uncapped (its double threshold
+// is evaluated for these edges only).
+__host__ __device__ __forceinline__ uint32_t count_floor(uint32_t du, uint32_t dv, const PivotTests& pt, double eps) {
+    float s = sqrtf(pt.tscale * (float)(du + 1u)) * 0.999999f;
+    s = s < 4.0e9f ? s : 4.0e9f;                       // eps > 1: keep the conversion defined
+    const uint32_t a = (uint32_t)s;
+    const uint32_t l = a > 2u ? a - 2u : 0u;
+    if (du + 1u <= 46340u) return l;
+    const double thr = eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u);
+    return thr >= 2147483648.0 ? l : (l < 46339u ? l : 46339u);
 }
 
 struct PredParams {
@@ -152,6 +167,7 @@ struct PredParams {
     double pq2;          // p^2 / q^2 rounded (an estimate only; infinity when p > q)
     float eps2_floor;    // min(p^2/q^2, eps*eps) as a float: within 2^-24 of a lower bound
                          // on the eps^2 of both predicates (count_floor's margin covers it)
+    uint32_t np_set;     // batched runs: the graph's prune-threshold table (its parameter set)
 };
 
 // Fill the derived fields; call after eps, p or q change.

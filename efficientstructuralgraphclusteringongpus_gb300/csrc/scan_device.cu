@@ -708,9 +708,13 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
     SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
-    if (prune && !per_graph) {   // batches: each pivot's graph has its own eps
+    if (prune && !per_graph) {
         k_prune_table<<<kPruneTable / 256, 256, 0, s>>>(pr, d->np_tab);
         pr.np_tab = d->np_tab;
+        ++*launches;
+    } else if (per_graph && bp->np_tabs) {   // one table per parameter set of the batch
+        k_prune_tables<<<dim3(kPruneTable / 256, kPruneSets), 256, 0, s>>>(bp->sets, bp->nsets, bp->np_tabs);
+        pr.np_tab = bp->np_tabs;
         ++*launches;
     }
     return per_graph ? launch_cn_impl<true>(d, launches, pr, fp) : launch_cn_impl<false>(d, launches, pr, fp);

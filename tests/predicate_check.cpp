@@ -2,7 +2,8 @@
 // against the per-edge double and 128-bit tests they replace in the counting kernels:
 //   * edge_pruned(du) == ref_f64_never(du, dv) && exact_never(du, dv)   for every du checked;
 //   * count_floor(du) <= exact_min_count and <= ref_min_count, and no count below it passes
-//     either predicate (ref_f64_similar, exact_similar).
+//     either predicate (ref_f64_similar, exact_similar); where the reference's int square of
+//     the count can wrap (du + 1 > 46340), every count below the bound is tried.
 // The same source is compiled for the device; host and device give the same bits here (IEEE
 // products, a correctly rounded sqrtf, no additions to contract).
 //
@@ -90,7 +91,7 @@ int main() {
                     return 1;
                 }
                 if (want || du + 1u > 46340u) continue;
-                const uint32_t fl = count_floor(du, pt);
+                const uint32_t fl = count_floor(du, dv, pt, pp.eps);
                 const uint32_t mx = exact_min_count(du, dv, pp.p, pp.q);
                 const uint32_t mr = ref_min_count(du, dv, pp.eps);
                 const uint32_t m = mx < mr ? mx : mr;
@@ -110,6 +111,31 @@ int main() {
             }
         }
     }
+    // The wrap zone: lower degree above 46339.  Every count below the bound must fail both
+    // predicates, the wrapped squares included.
+    uint64_t wrap_checks = 0;
+    for (const char* t : {"0.2", "0.4", "0.5", "0.9", "0.00005", "1"}) {
+        const Eps e = eps_of(t);
+        PredParams pp{e.eps, e.p, e.q, 1, 0.0, 0.f};
+        pred_derive(&pp);
+        for (uint32_t dv : {46340u, 50000u, 120000u, 290000u, 1151662u, 2000000000u}) {
+            const PivotTests pt = pivot_tests(dv, true, pp.eps, pp.p, pp.q, pp.pq2, pp.eps2_floor);
+            for (uint32_t du : {46340u, 46341u, 47000u, 60000u, 115000u, 290000u, 1151662u}) {
+                if (du > dv || edge_pruned(du, pt)) continue;
+                const uint32_t fl = count_floor(du, dv, pt, pp.eps);
+                const uint32_t top = fl < du ? fl : du;      // counts are below du
+                for (uint32_t c = 0; c < top; ++c) {
+                    ++wrap_checks;
+                    if (ref_f64_similar(c, du, dv, pp.eps) || exact_similar(c, du, dv, pp.p, pp.q)) {
+                        std::printf("FAIL wrap eps=%s dv=%u du=%u count=%u floor=%u\n", t, dv, du, c, fl);
+                        return 1;
+                    }
+                }
+            }
+        }
+    }
+    checks += wrap_checks;
+
     // eps with more than 9 decimals (ref-f64 runs only; GPUScan() passes the caller's double as
     // its shortest decimal): p^2 and q^2 wrap in 64 bits, so the exact side is not a test of
     // anything.  What the labels rest on must still hold: a pruned edge fails the reference's
@@ -127,7 +153,7 @@ int main() {
                     return 1;
                 }
                 if (edge_pruned(du, pt)) continue;
-                const uint32_t fl = count_floor(du, pt);
+                const uint32_t fl = count_floor(du, dv, pt, pp.eps);
                 if (fl > ref_min_count(du, dv, pp.eps) || (fl > 0 && ref_f64_similar(fl - 1, du, dv, pp.eps))) {
                     std::printf("FAIL long floor eps=%s dv=%u du=%u floor=%u\n", t, dv, du, fl);
                     return 1;
