@@ -256,7 +256,10 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 //     owner lane adds the hits that fell in its list from four ballots of the per-lane
 //     counts (0..8).
 constexpr uint32_t kLongWordsDefault = 32;   // lists of >= 128 entries take the whole warp (tunable)
-constexpr int kWordsInFlight = 2;        // hash kernel (48+ registers would cost occupancy)
+constexpr int kWordsInFlight = 2;        // hash and class kernels (48+ registers would cost occupancy)
+constexpr int kWordsInFlightMidHub = 3;  // k_cn_filter on mid hubs: two CTAs per SM by shared memory, so 64
+                                         // registers cost nothing (R-MAT s22: 11.87 -> 11.73 ms; 3 in the
+                                         // class kernels too: 12.11 ms)
 constexpr int kWordsInFlightBitmap = 6;  // bitmap kernel: one CTA per SM, 64 registers at 6 (s22: -0.6 ms against 4)
 
 __device__ __forceinline__ uint32_t lane_range_mask(int lo, int hi) {
@@ -687,9 +690,10 @@ __host__ __device__ constexpr size_t filter_smem_bytes(uint32_t entries) {
 // the rest finish the cheap batches and wait at the task barrier.
 // Two entry points share the body: k_cn_filter_classes (hash classes) is launch-bounded to
 // three 512-thread CTAs per SM, which holds it to 40 registers (R-MAT s22: the 4,096-entry
-// class 4.67 -> 4.25 ms); k_cn_filter (mid hubs, held to two CTAs per SM by their 112 KB of
-// shared memory) is left unbounded (48 registers; the bound measured slower there).
-template <bool kPerGraph>
+// class 4.67 -> 4.25 ms; two CTAs at 60 registers: slower again); k_cn_filter (mid hubs,
+// held to two CTAs per SM by their 112 KB of shared memory) is left unbounded and streams
+// three words per lane (64 registers; a bound measured slower there).
+template <bool kPerGraph, int W>
 __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t list_entries,
                             uint32_t* queue, const uint32_t* __restrict__ off,
                             const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
@@ -744,7 +748,7 @@ __device__ __forceinline__ void cn_filter_body(const CnTask* __restrict__ tasks,
             // tlo = 0: any count may be similar, so the bound decides nothing; count exactly
             const bool bound_scan = ue > ub && tlo > 0;
             uint32_t words = 0;
-            uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, bound_scan ? ue : ub, tlo, long_words, words,
+            uint32_t cnt = count_batch<W>(adj, lane, ub, bound_scan ? ue : ub, tlo, long_words, words,
                                                        [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
                                                            return filter_probe_word(x, p, lb, le, bits, log2bits);
                                                        });
@@ -777,7 +781,7 @@ __global__ void __launch_bounds__(512, 3) k_cn_filter_classes(const CnTask* __re
                             const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
                             uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
                             unsigned long long* __restrict__ ctr, FusedPred fp, uint32_t strided) {
-    cn_filter_body<kPerGraph>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
+    cn_filter_body<kPerGraph, kWordsInFlight>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
                               strided);
 }
 
@@ -787,7 +791,7 @@ __global__ void k_cn_filter(const CnTask* __restrict__ tasks, uint32_t ntasks, u
                             const uint32_t* __restrict__ adj, const uint32_t* __restrict__ lo_adj,
                             uint32_t* __restrict__ cn, uint32_t long_words, CnPrune pr,
                             unsigned long long* __restrict__ ctr, FusedPred fp, uint32_t strided) {
-    cn_filter_body<kPerGraph>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
+    cn_filter_body<kPerGraph, kWordsInFlightMidHub>(tasks, ntasks, list_entries, queue, off, adj, lo_adj, cn, long_words, pr, ctr, fp,
                               strided);
 }
 
