@@ -65,6 +65,8 @@ struct DeviceGraph {
     unsigned long long* cn_ctr = nullptr;
     uint32_t* task_queue = nullptr;        // launch_cn: one task counter per similarity kernel
     uint32_t* np_tab = nullptr;            // launch_cn: prune thresholds of pivot degrees < kPruneTable
+    uint32_t* miss = nullptr;              // split pivots' lower edges: misses found so far (one-shot runs)
+    uint32_t nmiss = 0, cap_miss = 0;
     bool has_split = false;                // the plan splits some pivot into chunks
     float* tau = nullptr;                  // served graphs: 2E similarity thresholds (k_tau)   // last launch_cn: [0] 16-byte list words read, [1] edges counted
     uint32_t* small_piv = nullptr;
@@ -88,7 +90,7 @@ struct DeviceGraph {
     bool cn_valid_before = false;
     RunScratch rs;                 // scratch of scan_run on this graph
     uint32_t* scratch = nullptr;   // scan tile sums, then dflags
-    uint32_t* dflags = nullptr;    // [0] input checks, [1..5] planner counters, [16] long lists
+    uint32_t* dflags = nullptr;    // [0] input checks, [1..8] planner counters, [16] long lists
     std::vector<std::pair<void*, size_t>> allocs;   // (pointer, bytes), returned to the cache on free
     uint64_t device_bytes = 0;     // device memory held by this graph
     uint32_t* adj_host = nullptr;  // streamed mode: pinned, GPU-mapped adjacency (adj points into it)

@@ -62,7 +62,8 @@ struct CnTask {
     uint32_t e0;     // edge slice [e0, e1) of the pivot
     uint32_t e1;
     uint32_t chunked;  // 1 when N(v) is split (partial counts are added atomically)
-    uint32_t pad0, pad1;
+    uint32_t mofs;     // chunked: edge k's slot in the miss counters is k + mofs (mod 2^32)
+    uint32_t pad1;
 };
 
 // Insert w into a table of `cap` slots (never full: load <= 1/4).
@@ -553,14 +554,18 @@ __device__ __forceinline__ uint32_t next_task(uint32_t* queue, uint32_t prev, bo
 __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint32_t cap, uint32_t* queue,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
                          const uint32_t* __restrict__ lo_adj, uint32_t* __restrict__ cn, uint32_t long_words,
-                         CnPrune pr, unsigned long long* __restrict__ ctr) {
+                         CnPrune pr, unsigned long long* __restrict__ ctr, uint32_t* __restrict__ miss,
+                         uint32_t nmiss, uint32_t stride) {
     extern __shared__ __align__(16) uint32_t tab[];
     __shared__ uint32_t next_batch, task_slot;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nb = cap / 4;
     for (uint32_t t = next_task(queue, 0, true, &task_slot); t < ntasks;
          t = next_task(queue, t, false, &task_slot)) {
-        const CnTask tk = tasks[t];
+        // stride (coprime to ntasks, 0: in order): the i-th task drawn is i * stride mod ntasks,
+        // so the chunks of one split pivot, adjacent in the array, run spread over the launch
+        // and the misses of the early ones can decide edges for the later ones
+        const CnTask tk = tasks[stride ? (uint32_t)((uint64_t)t * stride % ntasks) : t];
         for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
             reinterpret_cast<uint4*>(tab)[i] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
         if (threadIdx.x == 0) next_batch = 0;
@@ -578,7 +583,7 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
             if (kb >= tk.e1) break;
             const uint32_t k = kb + lane;
             const bool valid = k < tk.e1;
-            uint32_t ub = 0, ue = 0, u = 0, du = 0;
+            uint32_t ub = 0, ue = 0, u = 0, du = 0, tlo = 0, mi = 0xFFFFFFFFu;
             bool counted = false;
             if (valid) {
                 u = lo_adj[k];
@@ -587,12 +592,29 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 du = ue - ub;
                 if (edge_pruned(du, pt)) ue = ub;
                 counted = ue > ub && tk.cb == vb;               // once per edge: in its first chunk
+                if (pr.on && ue > ub) tlo = count_floor(du, ve - vb, pt, pr.eps);
                 if (tk.chunked && ue > ub) {
-                    if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
-                    if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
+                    // One-shot runs: the misses found by the edge's other chunks so far bound
+                    // its count by du - misses; once that is below tlo the edge is decided and
+                    // its other chunks skip it.  Stale reads only weaken the bound.
+                    uint32_t pot = du;
+                    if (tlo && miss && k + tk.mofs < nmiss) {
+                        mi = k + tk.mofs;
+                        const uint32_t m = __ldcg(miss + mi);
+                        pot = m >= du ? 0u : du - m;
+                    }
+                    if (pot < tlo) {
+                        ue = ub;
+                    } else {
+                        if (lo_id) ub = lower_bound_u32(adj, ub, ue, lo_id);
+                        if (hi_id != kEmpty) ue = lower_bound_u32(adj, ub, ue, hi_id + 1);
+                        // hits this chunk must still find for the edge to reach tlo; 0: none
+                        // decides it here, so the chunk counts its sub-list in full
+                        const uint64_t outside = (uint64_t)pot - (ue - ub);
+                        tlo = mi != 0xFFFFFFFFu && tlo > outside ? (uint32_t)(tlo - outside) : 0u;
+                    }
                 }
             }
-            const uint32_t tlo = (pr.on && !tk.chunked && ue > ub) ? count_floor(du, ve - vb, pt, pr.eps) : 0u;
             uint32_t words = 0;
             const uint32_t cnt = count_batch<kWordsInFlight>(adj, lane, ub, ue, tlo, long_words, words,
                                                              [&](uint4 x, uint32_t p, uint32_t lb, uint32_t le) {
@@ -604,8 +626,17 @@ __global__ void k_cn_big(const CnTask* __restrict__ tasks, uint32_t ntasks, uint
                 atomicAdd(&ctr[1], (unsigned long long)nc);
             }
             if (valid) {
-                if (!tk.chunked) cn[k] = cnt;
-                else if (cnt) atomicAdd(&cn[k], cnt);           // cn was zeroed before the launch
+                if (!tk.chunked) {
+                    cn[k] = cnt;
+                } else {
+                    if (cnt) atomicAdd(&cn[k], cnt);            // cn was zeroed before the launch
+                    if (mi != 0xFFFFFFFFu && ue > ub) {
+                        // below its threshold the chunk decided the edge (stopped early, or read
+                        // in full with too few hits); otherwise it read all ue - ub entries
+                        if (tlo && cnt < tlo) atomicMax(miss + mi, du);
+                        else if (ue - ub > cnt) atomicAdd(miss + mi, ue - ub - cnt);
+                    }
+                }
             }
         }
         __syncthreads();
@@ -942,7 +973,10 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
                 const uint32_t smax = (L + pp.min_slice_edges - 1) / pp.min_slice_edges;
                 nsl = (uint32_t)(s < 1 ? 1 : (s > smax ? smax : s));
                 ntask = nch * nsl;
-                if (nch > 1 && small_out == nullptr) atomicAdd(&counts[kClasses], 1u);   // split pivots
+                if (nch > 1 && small_out == nullptr) {
+                    atomicAdd(&counts[kClasses], 1u);       // split pivots
+                    atomicAdd(&counts[kClasses + 1], L);    // ... and their lower edges (miss counters)
+                }
             }
         }
     }
@@ -959,6 +993,7 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
     }
     CnTask* out = cls == 1 ? big0 : cls == 2 ? big1 : cls == 3 ? big2 : cls == 4 ? bmp : hmid;
     const uint32_t vb = off[v], e0 = lo_off[v];
+    const uint32_t mbase = nch > 1 ? atomicAdd(&counts[kClasses + 1], L) : 0u;   // this pivot's miss counters
     uint32_t i = 0;
     for (uint32_t c = 0; c < nch; ++c) {
         const uint32_t cb = vb + (uint32_t)((uint64_t)dv * c / nch);
@@ -971,7 +1006,8 @@ __global__ void k_plan(uint32_t n, const uint32_t* __restrict__ off, const uint3
             t.e0 = e0 + (uint32_t)((uint64_t)L * s / nsl);
             t.e1 = e0 + (uint32_t)((uint64_t)L * (s + 1) / nsl);
             t.chunked = nch > 1;
-            t.pad0 = t.pad1 = 0;
+            t.mofs = mbase - e0;
+            t.pad1 = 0;
             out[pos + i] = t;
         }
     }

@@ -299,10 +299,10 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
     cudaStream_t s = d->stream;
     uint32_t* counts = d->dflags + 1;
     const unsigned pg = (unsigned)((d->n + 255) / 256);
-    SCAN_CUDA(cudaMemsetAsync(counts, 0, (4 + kNumBigClasses) * sizeof(uint32_t), s));
+    SCAN_CUDA(cudaMemsetAsync(counts, 0, (5 + kNumBigClasses) * sizeof(uint32_t), s));
     k_plan<<<pg, 256, 0, s>>>(d->n, d->off, d->lo_off, d->work, d->tailc, pp, counts, nullptr, nullptr, nullptr,
                               nullptr, nullptr, nullptr);
-    uint32_t hc[4 + kNumBigClasses];
+    uint32_t hc[5 + kNumBigClasses];
     SCAN_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     SCAN_CUDA(cudaStreamSynchronize(s));
     // task arrays: reuse the current ones when large enough
@@ -321,6 +321,8 @@ scan_status plan_tasks(DeviceGraph* d, const PlanParams& pp) {
     d->nbmp = hc[1 + kNumBigClasses];
     d->nhmid = hc[2 + kNumBigClasses];
     d->has_split = hc[3 + kNumBigClasses] > 0;
+    d->nmiss = hc[4 + kNumBigClasses];               // lower edges of split pivots
+    if (d->nmiss) SCAN_TRY(ensure(&d->miss, &d->cap_miss, d->nmiss));
     SCAN_TRY(ensure(&d->hubs, &d->cap_hubs, d->nhmid + d->nbmp));   // mid hubs, then the larger hubs
     d->hmid = d->hubs;
     d->bmp = d->hubs + d->nhmid;
@@ -564,6 +566,16 @@ static int g_per_sm_hub_filter[64][2] = {};                 // k_cn_filter on th
 static int g_per_sm_filter[64][2][kNumBigClasses][2] = {};  // k_cn_filter, [g][class][largest class 2
                                                             // at the default chunk, or at the cap]
 
+// A stride coprime to n near n / golden ratio: i * stride mod n visits 0..n-1 once each,
+// consecutive draws far apart in the array (k_cn_big's order for split pivots).
+static uint32_t spread_stride(uint32_t n) {
+    if (n < 3) return 0;
+    uint64_t st = (uint64_t)(n * 0.6180339887);
+    auto gcd = [](uint64_t a, uint64_t b) { while (b) { const uint64_t r = a % b; a = b; b = r; } return a; };
+    while (gcd(st, n) != 1) ++st;
+    return (uint32_t)st;
+}
+
 template <bool kPerGraph>
 static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPrune& pr, const FusedPred& fp) {
     cudaStream_t s = d->stream;
@@ -661,7 +673,8 @@ static scan_status launch_cn_impl(DeviceGraph* d, uint32_t* launches, const CnPr
                 k_cn_big<<<(unsigned)grid, threads, smem, s>>>(d->big[c], d->nbig[c], big_class_slots(c),
                                                                 d->task_queue + c, d->off,
                                                                 d->adj, d->lo_adj, d->cn, d->long_words, pr,
-                                                                d->cn_ctr);
+                                                                d->cn_ctr, pr.on ? d->miss : nullptr, d->nmiss,
+                                                                pr.on && d->nmiss ? spread_stride(d->nbig[c]) : 0u);
             }
             ++*launches;
         }
@@ -708,6 +721,7 @@ scan_status launch_cn(DeviceGraph* d, uint32_t* launches, const PredParams* prun
     SCAN_CUDA(cudaMemsetAsync(d->cn, 0, d->E * sizeof(uint32_t), s));
     SCAN_CUDA(cudaMemsetAsync(d->cn_ctr, 0, 2 * sizeof(unsigned long long), s));
     SCAN_CUDA(cudaMemsetAsync(d->task_queue, 0, 8 * sizeof(uint32_t), s));
+    if (prune && d->nmiss) SCAN_CUDA(cudaMemsetAsync(d->miss, 0, (size_t)d->nmiss * sizeof(uint32_t), s));
     if (prune && !per_graph) {
         k_prune_table<<<kPruneTable / 256, 256, 0, s>>>(pr, d->np_tab);
         pr.np_tab = d->np_tab;
