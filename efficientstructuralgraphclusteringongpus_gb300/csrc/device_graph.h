@@ -53,7 +53,9 @@ struct DeviceGraph {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;   // the hub kernels of the similarity stage, beside the classes
+    cudaStream_t aux = nullptr;    // upload: orientation passes beside the adjacency copy
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t chunk_ev[9] = {};  // upload: one per adjacency chunk, and the end of the aux stream
     uint32_t n = 0;
     uint64_t m = 0, E = 0;
     uint32_t* off = nullptr;

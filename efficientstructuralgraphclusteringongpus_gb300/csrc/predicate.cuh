@@ -149,14 +149,20 @@ __host__ __device__ __forceinline__ bool edge_pruned(uint32_t du, const PivotTes
 // below which the square is exact.  When the reference's threshold is 2^31 or more, no
 // square, wrapped or not, reaches it, and the bound is left uncapped (its double threshold
 // is evaluated for these edges only).
+// Out of line, so that the compiler does not evaluate its double products for every edge
+// (if-converted, they kept GB300's FP64 pipe 8.5% busy in the 1,024-entry class).
+static __host__ __device__ __noinline__ uint32_t wrap_zone_floor(uint32_t l, uint32_t du, uint32_t dv, double eps) {
+    const double thr = eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u);
+    return thr >= 2147483648.0 ? l : (l < 46339u ? l : 46339u);
+}
+
 __host__ __device__ __forceinline__ uint32_t count_floor(uint32_t du, uint32_t dv, const PivotTests& pt, double eps) {
     float s = sqrtf(pt.tscale * (float)(du + 1u)) * 0.999999f;
     s = s < 4.0e9f ? s : 4.0e9f;                       // eps > 1: keep the conversion defined
     const uint32_t a = (uint32_t)s;
     const uint32_t l = a > 2u ? a - 2u : 0u;
     if (du + 1u <= 46340u) return l;
-    const double thr = eps * eps * (double)(int32_t)(du + 1u) * (double)(int32_t)(dv + 1u);
-    return thr >= 2147483648.0 ? l : (l < 46339u ? l : 46339u);
+    return wrap_zone_floor(l, du, dv, eps);
 }
 
 struct PredParams {

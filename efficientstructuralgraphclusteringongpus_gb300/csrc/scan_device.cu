@@ -168,20 +168,96 @@ static void cache_give(int dev, void* p, size_t bytes) {
     g_cache_bytes[dev] += bytes;
 }
 
+// Streams and events of a resident graph come from a per-device pool and go back to it
+// when the graph is freed, so that a GPUScan() call (upload, run, free) creates and destroys
+// none of its 3 streams and 29 events.
+struct StreamSet {
+    cudaStream_t stream, side, aux;
+    cudaEvent_t fork, join, ev[16], chunk_ev[9];
+};
+static std::mutex g_ss_mu;
+static std::vector<StreamSet> g_ss_pool[64];
+constexpr size_t kStreamSetPool = 8;
+
+static void destroy_streams(const StreamSet& x) {
+    for (cudaStream_t st : {x.stream, x.side, x.aux})
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : {x.fork, x.join})
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : x.ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : x.chunk_ev)
+        if (e) cudaEventDestroy(e);
+}
+
+static StreamSet streams_of(const DeviceGraph* d) {
+    StreamSet x{d->stream, d->side, d->aux, d->fork, d->join, {}, {}};
+    std::copy(std::begin(d->ev), std::end(d->ev), x.ev);
+    std::copy(std::begin(d->chunk_ev), std::end(d->chunk_ev), x.chunk_ev);
+    return x;
+}
+
+// The current device must be d->device.
+static scan_status take_streams(DeviceGraph* d) {
+    StreamSet x{};
+    bool pooled = false;
+    {
+        std::lock_guard<std::mutex> lock(g_ss_mu);
+        auto& pool = g_ss_pool[d->device];
+        if (!pool.empty()) {
+            x = pool.back();
+            pool.pop_back();
+            pooled = true;
+        }
+    }
+    if (!pooled) {
+        auto make = [&]() -> cudaError_t {
+            cudaError_t e = cudaSuccess;
+            for (cudaStream_t* st : {&x.stream, &x.side, &x.aux})
+                if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+            for (cudaEvent_t* ev : {&x.fork, &x.join})
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+            for (auto& ev : x.ev)
+                if (e == cudaSuccess) e = cudaEventCreate(&ev);
+            for (auto& ev : x.chunk_ev)
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            return e;
+        };
+        const cudaError_t e = make();
+        if (e != cudaSuccess) {
+            destroy_streams(x);
+            return fail(SCAN_ERR_CUDA, std::string("stream/event creation: ") + cudaGetErrorString(e));
+        }
+    }
+    d->stream = x.stream;
+    d->side = x.side;
+    d->aux = x.aux;
+    d->fork = x.fork;
+    d->join = x.join;
+    std::copy(std::begin(x.ev), std::end(x.ev), d->ev);
+    std::copy(std::begin(x.chunk_ev), std::end(x.chunk_ev), d->chunk_ev);
+    return SCAN_OK;
+}
+
 void device_graph_free(DeviceGraph* d) {
     if (!d) return;
     int prev = -1;
     cudaGetDevice(&prev);
     if (d->device >= 0) cudaSetDevice(d->device);
-    if (d->stream) cudaStreamSynchronize(d->stream);
+    // the aux and side streams' last work is joined into the main stream
+    const bool idle = d->stream && cudaStreamSynchronize(d->stream) == cudaSuccess;
     for (auto& a : d->allocs) cache_give(d->device, a.first, a.second);
     if (d->adj_host) cudaFreeHost(d->adj_host);
-    for (auto& e : d->ev)
-        if (e) cudaEventDestroy(e);
-    if (d->stream) cudaStreamDestroy(d->stream);
-    if (d->side) cudaStreamDestroy(d->side);
-    if (d->fork) cudaEventDestroy(d->fork);
-    if (d->join) cudaEventDestroy(d->join);
+    const StreamSet x = streams_of(d);
+    bool kept = false;
+    if (idle && d->device >= 0 && d->device < 64 && x.stream && x.side && x.aux) {
+        std::lock_guard<std::mutex> lock(g_ss_mu);
+        if (g_ss_pool[d->device].size() < kStreamSetPool) {
+            g_ss_pool[d->device].push_back(x);
+            kept = true;
+        }
+    }
+    if (!kept) destroy_streams(x);
     if (prev >= 0) cudaSetDevice(prev);
     delete d;
 }
@@ -344,11 +420,7 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     d->n = (uint32_t)n;
     d->m = m;
     SCAN_CUDA(cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, device));
-    SCAN_CUDA(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
-    SCAN_CUDA(cudaStreamCreateWithFlags(&d->side, cudaStreamNonBlocking));
-    SCAN_CUDA(cudaEventCreateWithFlags(&d->fork, cudaEventDisableTiming));
-    SCAN_CUDA(cudaEventCreateWithFlags(&d->join, cudaEventDisableTiming));
-    for (auto& e : d->ev) SCAN_CUDA(cudaEventCreate(&e));
+    SCAN_TRY(take_streams(d.get()));
     cudaStream_t s = d->stream;
 
     SCAN_TRY(dalloc(d.get(), &d->off, n + 1));
@@ -430,15 +502,10 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     // hot-id mapping and orientation count (one pass, k_orient_tiles) run on a second stream
     // while the next chunk is copied.  The pass skips ids >= n, so no host check has to come
     // in between; the flags are read once, after the count.
-    cudaStream_t s2 = nullptr;
-    SCAN_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    cudaStream_t s2 = d->aux;
     constexpr int kMaxChunks = 8;
-    cudaEvent_t ev_chunk[kMaxChunks + 1] = {};
-    auto cleanup = [&] {
-        for (auto& e : ev_chunk)
-            if (e) cudaEventDestroy(e);
-        cudaStreamDestroy(s2);
-    };
+    static_assert(kMaxChunks + 1 <= sizeof(d->chunk_ev) / sizeof(d->chunk_ev[0]), "one event per chunk and one more");
+    cudaEvent_t* ev_chunk = d->chunk_ev;
     const int chunks = (adj_in_host_memory || m < (16ull << 20)) ? 1 : kMaxChunks;
     std::vector<uint32_t> vcut(chunks + 1, 0);
     vcut[chunks] = (uint32_t)n;
@@ -456,7 +523,6 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     scan_status ost = SCAN_OK;
     uint32_t orient_launches = 0;
     auto enqueue = [&]() -> scan_status {
-        for (auto& e : ev_chunk) SCAN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         // on s2, needing only the offsets (already on the device)
         SCAN_CUDA(cudaMemsetAsync(lowbits, 0, (m / 32 + 2) * sizeof(uint32_t), s2));
         SCAN_CUDA(cudaMemsetAsync(cnt, 0, n * sizeof(uint32_t), s2));
@@ -496,10 +562,8 @@ scan_status device_upload(int device, uint64_t n, uint64_t m, const void* off_ho
     ost = enqueue();
     if (ost != SCAN_OK) {
         cudaStreamSynchronize(s2);
-        cleanup();
         return ost;
     }
-    cleanup();   // pending work on s2 completes; s waits on its last event
     SCAN_TRY(device_scan(d.get(), cnt, n, d->lo_off, d->scratch));
     uint32_t E32 = 0;
     SCAN_CUDA(cudaMemcpyAsync(&E32, d->lo_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -19,6 +19,7 @@
 #define __host__
 #define __device__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 #include "predicate.cuh"
 
 using namespace scan;
