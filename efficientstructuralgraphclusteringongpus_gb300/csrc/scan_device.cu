@@ -201,7 +201,7 @@ static StreamSet streams_of(const DeviceGraph* d) {
 static scan_status take_streams(DeviceGraph* d) {
     StreamSet x{};
     bool pooled = false;
-    {
+    if (d->device >= 0 && d->device < 64) {
         std::lock_guard<std::mutex> lock(g_ss_mu);
         auto& pool = g_ss_pool[d->device];
         if (!pool.empty()) {
